@@ -1,0 +1,189 @@
+"""Generate golden vectors by running the reference solver itself (float64, CPU).
+
+Run in a container where the reference project is checked out:
+
+    PYTHONPATH=<reference checkout> python tests/golden/make_golden.py <reference checkout>
+
+It imports ``hydrointel`` from the given checkout, drives the reference's own
+SWE2D / SWE1D / exchange / CoupledEngine on small seeded cases and writes
+``tests/golden/*.npz``.  The cases are defined in ``golden_cases.py`` (shared with
+the tests, so that forcing callables are rebuilt identically).  The fixtures are
+committed; nothing at test time reads the reference.
+"""
+from __future__ import annotations
+
+import math
+import sys
+from pathlib import Path
+
+import numpy as np
+
+HERE = Path(__file__).resolve().parent
+sys.path.insert(0, str(HERE))
+import golden_cases as GC  # noqa: E402
+
+
+def _t(x):
+    import torch
+    return x.detach().cpu().numpy().astype(np.float64) if torch.is_tensor(x) else np.asarray(x, dtype=np.float64)
+
+
+def make_swe2d(name: str, ref):
+    import torch
+    from hydrointel.config import SolverConfig
+    from hydrointel.solver.boundaries import EdgeBC
+    from hydrointel.solver.infiltration import Horton
+    from hydrointel.solver.swe2d import SWE2D
+    spec = GC.SWE2D_CASES[name]
+    inp = GC.swe2d_inputs(spec)
+    cfg = SolverConfig(spatial_order=spec["order"], flux=spec["flux"], compile=False)
+    bcs = {e: EdgeBC(k, GC.bc_value(spec, e)) for e, k in zip(GC.EDGES, spec["bc"])}
+    horton = None
+    if inp.get("f0") is not None:
+        horton = Horton(torch.as_tensor(inp["f0"]), torch.as_tensor(inp["fc"]), torch.as_tensor(inp["k"]),
+                        spec["t0"])
+    sim = SWE2D(inp["z"], inp["n"], spec["dx"], cfg, bcs, torch.device("cpu"), torch.float64,
+                storage=inp.get("S"), horton=horton, rain_weight=inp.get("rain_weight"), dy=spec.get("dy"),
+                batch=spec.get("batch"))
+    sim.set_state(inp["h0"], inp["hu0"], inp["hv0"])
+    rec = {k: [] for k in ("dt", "t", "rate", "bnd_in", "bnd_out", "rain", "infil", "clip")}
+    snaps = {}
+    t = 0.0
+    for k in range(spec["steps"]):
+        rate = float(sim._max_rate(sim.h, sim.hu, sim.hv))
+        dt = min(sim.max_dt(), spec.get("dt_cap", 1e9))
+        vol = sim.step(dt, t, GC.rain_value(spec, t))
+        rec["dt"].append(dt); rec["t"].append(t); rec["rate"].append(rate)
+        for key, val in zip(("bnd_in", "bnd_out", "rain", "infil", "clip"),
+                            (vol.bnd_in, vol.bnd_out, vol.rain, vol.infil, vol.clip)):
+            rec[key].append(_t(val).reshape(-1))
+        t += dt
+        if k + 1 in spec["snap_at"]:
+            for f in ("h", "hu", "hv", "s_filled", "infil_cum"):
+                snaps[f"{f}_{k + 1}"] = _t(getattr(sim, f))
+    out = {k: np.asarray(v) for k, v in rec.items()}
+    out.update(snaps)
+    out.update({f"in_{k}": np.asarray(v) for k, v in inp.items() if v is not None})
+    np.savez_compressed(HERE / f"{name}.npz", **out)
+    print(name, "steps", spec["steps"], "final t", t)
+
+
+def make_swe1d(name: str):
+    import torch
+    from hydrointel.config import SolverConfig
+    from hydrointel.domain.channels import apply_gamma
+    from hydrointel.solver.swe1d import SWE1D
+    spec = GC.SWE1D_CASES[name]
+    cfg = SolverConfig(compile=False, slot_width_frac=spec["slot_width_frac"])
+    net = GC.network(spec)
+    B = spec.get("batch")
+    nets = [apply_gamma(net, np.asarray(g)) for g in spec["gammas"]] if B else net
+    one = SWE1D(nets, cfg, torch.device("cpu"), torch.float64, inflow=GC.inflow_fn(spec), stage=GC.stage_fn(spec))
+    one.set_level(torch.maximum(one.z + spec["init_depth"], torch.full_like(one.z, GC.stage_fn(spec)(0.0)
+                                                                           if B is None else -1e9)))
+    tp = one.topo
+    out = {f"topo_{k}": np.asarray(getattr(tp, k)) for k in ("kind", "reach_of", "ghost_src", "ghost_sign",
+                                                              "face_l", "face_r", "z", "b", "m", "zbank", "n",
+                                                              "dx", "x", "y", "chain")}
+    out["n_cells"] = np.asarray(tp.n_cells)
+    for k in ("b", "m", "yb", "ts"):
+        out[f"sec_{k}"] = _t(getattr(one.sec, k))
+        out[f"fsec_{k}"] = _t(getattr(one.fsec, k))
+    out["z_members"] = _t(one.z)
+    out["A0"], out["Q0"] = _t(one.A), _t(one.Q)
+    rec = {k: [] for k in ("dt", "t", "max_dt", "bnd_in", "bnd_out", "clip")}
+    t = 0.0
+    for k in range(spec["steps"]):
+        mdt = one.max_dt()
+        dt = mdt * spec.get("dt_frac", 1.0)
+        v = one.step(dt, t)
+        rec["dt"].append(dt); rec["t"].append(t); rec["max_dt"].append(mdt)
+        rec["bnd_in"].append(_t(v.bnd_in).reshape(-1)); rec["bnd_out"].append(_t(v.bnd_out).reshape(-1))
+        rec["clip"].append(_t(v.clip).reshape(-1))
+        t += dt
+        if k + 1 in spec["snap_at"]:
+            out[f"A_{k + 1}"], out[f"Q_{k + 1}"] = _t(one.A), _t(one.Q)
+    out.update({k: np.asarray(v) for k, v in rec.items()})
+    np.savez_compressed(HERE / f"{name}.npz", **out)
+    print(name, "cells", tp.n_cells, "final t", t)
+
+
+def make_exchange(name: str):
+    import torch
+    from hydrointel.benchmarks.suite import _overtopping_case
+    from hydrointel.solver.coupling import exchange
+    spec = GC.EXCHANGE_CASES[name]
+    eng, one, two = _overtopping_case(torch.device("cpu"), dx=spec["dx"])
+    L = eng.links
+    out = {"links_cell1d": _t(L.cell1d).astype(np.int64), "links_zbank": _t(L.zbank),
+           "links_length": _t(L.length), "links_z2": _t(L.z2), "links_inv": _t(L.inv).astype(np.int64),
+           "links_uniq": _t(L.uniq_dev).astype(np.int64), "z2d": _t(two.z), "z1d": _t(one.z),
+           "dx1": _t(one.dx), "area2": np.asarray(two.area)}
+    for k in ("b", "m", "yb", "ts"):
+        out[f"sec_{k}"] = _t(getattr(one.sec, k))
+    for k in ("kind", "reach_of", "ghost_src", "ghost_sign", "face_l", "face_r", "z", "b", "m", "zbank", "n",
+              "dx", "x", "y", "chain"):
+        out[f"topo_{k}"] = np.asarray(getattr(one.topo, k))
+    out["n_cells"] = np.asarray(one.topo.n_cells)
+    out["n2d"] = _t(two.n)
+    g = torch.Generator().manual_seed(spec["seed"])
+    for i in range(spec["calls"]):
+        two.set_state(torch.rand(two.z.shape, generator=g, dtype=torch.float64) * 1.5)
+        two.hu = torch.rand(two.z.shape, generator=g, dtype=torch.float64) - 0.5
+        two.hv = torch.rand(two.z.shape, generator=g, dtype=torch.float64) - 0.5
+        one.A = one.sec.area(torch.rand(one.z.shape, generator=g, dtype=torch.float64) * 4.0)
+        out[f"h_in_{i}"], out[f"hu_in_{i}"], out[f"hv_in_{i}"] = _t(two.h), _t(two.hu), _t(two.hv)
+        out[f"A_in_{i}"] = _t(one.A)
+        V = exchange(one, two, L, spec["dt"], eng.cfg)
+        out[f"V_{i}"] = _t(V)
+        out[f"h_out_{i}"], out[f"hu_out_{i}"], out[f"hv_out_{i}"] = _t(two.h), _t(two.hu), _t(two.hv)
+        out[f"A_out_{i}"] = _t(one.A)
+    np.savez_compressed(HERE / f"{name}.npz", **out)
+    print(name, "links", len(L.cell1d))
+
+
+def make_coupled(name: str):
+    import torch
+    from hydrointel.benchmarks.suite import _overtopping_case
+    spec = GC.COUPLED_CASES[name]
+    eng, one, two = _overtopping_case(torch.device("cpu"), dx=spec["dx"])
+    eng.rain = GC.rain_fn_coupled(spec)
+    two.set_state(np.asarray(GC.coupled_h0(spec, _t(two.z))))
+    eng.mb = type(eng.mb)(two.device, eng.total_volume())
+    rec = {k: [] for k in ("dt", "n_sub", "t")}
+    t = 0.0
+    out = {"h0": _t(two.h), "A0": _t(one.A), "Q0": _t(one.Q)}
+    for k in range(spec["steps"]):
+        dt = min(two.max_dt(), spec["t_end"] - t)
+        n_sub = max(1, math.ceil(dt / one.max_dt() - 1e-9))
+        rec["dt"].append(dt); rec["n_sub"].append(n_sub); rec["t"].append(t)
+        t = eng.step(t, spec["t_end"], dt=dt, n_sub=n_sub)
+        if k + 1 in spec["snap_at"]:
+            out[f"h_{k + 1}"], out[f"hu_{k + 1}"], out[f"hv_{k + 1}"] = _t(two.h), _t(two.hu), _t(two.hv)
+            out[f"A_{k + 1}"], out[f"Q_{k + 1}"] = _t(one.A), _t(one.Q)
+    src = eng.mb.sources()
+    for k, v in src.items():
+        out[f"src_{k}"] = np.asarray(v, dtype=np.float64)
+    out["mass_err"] = np.asarray(eng.mb.check(eng.total_volume(), t, record=False))
+    out.update({k: np.asarray(v) for k, v in rec.items()})
+    np.savez_compressed(HERE / f"{name}.npz", **out)
+    print(name, "steps", spec["steps"], "final t", t, "mass err", float(out["mass_err"]))
+
+
+def main(argv):
+    ref = Path(argv[1] if len(argv) > 1 else "/root/reference")
+    sys.path.insert(0, str(ref))
+    import torch
+    torch.set_num_threads(1)
+    for name in GC.SWE2D_CASES:
+        make_swe2d(name, ref)
+    for name in GC.SWE1D_CASES:
+        make_swe1d(name)
+    for name in GC.EXCHANGE_CASES:
+        make_exchange(name)
+    for name in GC.COUPLED_CASES:
+        make_coupled(name)
+
+
+if __name__ == "__main__":
+    main(sys.argv)

@@ -1,0 +1,91 @@
+"""Test harness: builds oracle objects (and, on a GPU, the CUDA engine's objects) for the
+golden cases, from the committed fixtures and the shared case definitions."""
+from __future__ import annotations
+
+from pathlib import Path
+from types import SimpleNamespace
+
+import numpy as np
+
+import golden_cases as GC
+from his_gb300.boundaries import EdgeBC
+from his_gb300.config import SolverConfig
+
+GOLDEN = Path(__file__).resolve().parent / "golden"
+
+
+def load(name: str) -> dict:
+    with np.load(GOLDEN / f"{name}.npz") as f:
+        return {k: f[k] for k in f.files}
+
+
+def swe2d_cfg(spec) -> SolverConfig:
+    return SolverConfig(spatial_order=spec["order"], flux=spec["flux"])
+
+
+def swe2d_bcs(spec) -> dict:
+    return {e: EdgeBC(k, GC.bc_value(spec, e)) for e, k in zip(GC.EDGES, spec["bc"])}
+
+
+def swe2d_inputs(name: str, fx: dict) -> dict:
+    g = lambda k: fx.get(f"in_{k}")
+    return {k: g(k) for k in ("z", "n", "S", "f0", "fc", "k", "rain_weight", "h0", "hu0", "hv0")}
+
+
+def oracle_swe2d(name: str, fx: dict | None = None):
+    from oracle.oracle import OracleSWE2D
+    spec = GC.SWE2D_CASES[name]
+    fx = fx if fx is not None else load(name)
+    inp = swe2d_inputs(name, fx)
+    horton = (inp["f0"], inp["fc"], inp["k"], spec["t0"]) if inp["f0"] is not None else None
+    sim = OracleSWE2D(inp["z"], inp["n"], spec["dx"], swe2d_cfg(spec), swe2d_bcs(spec), storage=inp["S"],
+                      horton=horton, rain_weight=inp["rain_weight"], dy=spec.get("dy"), batch=spec.get("batch"))
+    sim.set_state(inp["h0"], inp["hu0"], inp["hv0"])
+    return sim, spec, fx
+
+
+def topo_from(fx: dict) -> SimpleNamespace:
+    keys = ("kind", "reach_of", "ghost_src", "ghost_sign", "face_l", "face_r", "z", "b", "m", "zbank", "n", "dx",
+            "x", "y", "chain")
+    t = SimpleNamespace(**{k: fx[f"topo_{k}"] for k in keys})
+    t.n_cells = int(fx["n_cells"])
+    return t
+
+
+def oracle_swe1d(name: str, fx: dict | None = None):
+    from oracle.oracle import OracleSWE1D
+    spec = GC.SWE1D_CASES[name]
+    fx = fx if fx is not None else load(name)
+    cfg = SolverConfig(slot_width_frac=spec["slot_width_frac"])
+    topo = topo_from(fx)
+    one = OracleSWE1D(topo, cfg, batch=spec.get("batch"), z=fx["z_members"], b=fx["sec_b"],
+                      inflow=GC.inflow_fn(spec), stage=GC.stage_fn(spec))
+    one.A = np.ascontiguousarray(fx["A0"].reshape(one.A.shape))
+    one.Q = np.ascontiguousarray(fx["Q0"].reshape(one.Q.shape))
+    return one, spec, fx
+
+
+def overtop_parts(fx: dict, cfg: SolverConfig | None = None):
+    """The reference's overtopping case (benchmarks/suite.py:406-431) rebuilt from the exchange fixture:
+    1-D topology, 2-D bed and roughness, links and forcing."""
+    cfg = cfg or SolverConfig()
+    topo = topo_from(fx)
+    zb_last = float(fx["topo_zbank"][fx["topo_kind"] == 0][-1])
+    return SimpleNamespace(cfg=cfg, topo=topo, z2d=fx["z2d"], n2d=fx["n2d"], dx=float(np.sqrt(fx["area2"])),
+                           inflow=GC.overtop_inflow, stage=lambda t: zb_last - 1.0,
+                           links={k: fx[f"links_{k}"] for k in ("cell1d", "zbank", "length", "z2", "inv", "uniq")})
+
+
+def oracle_overtop(fx: dict, cfg: SolverConfig | None = None):
+    from oracle.oracle import OracleLinks, OracleSWE1D, OracleSWE2D
+    from his_gb300.boundaries import all_edges
+    p = overtop_parts(fx, cfg)
+    two = OracleSWE2D(p.z2d, p.n2d, p.dx, p.cfg, all_edges("closed"))
+    one = OracleSWE1D(p.topo, p.cfg, inflow=p.inflow, stage=p.stage)
+    links = OracleLinks(**p.links)
+    return one, two, links, p
+
+
+def max_abs(a, b) -> float:
+    a, b = np.asarray(a, dtype=np.float64), np.asarray(b, dtype=np.float64)
+    return float(np.max(np.abs(a - b))) if a.size else 0.0
