@@ -1,0 +1,463 @@
+// C ABI of the flood-engine step (include/his_gb300.h): argument checks, device
+// tables, host<->device parameter and result movement, precision dispatch.
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "his_internal.h"
+
+namespace his {
+
+static thread_local std::string g_last_error;
+
+void set_error(const std::string& msg) { g_last_error = msg; }
+
+int cuda_fail(cudaError_t e, const char* what) {
+    g_last_error = std::string(what) + ": " + cudaGetErrorString(e);
+    return HIS_ERR_CUDA;
+}
+
+const TileShape kTileShapes[] = {{32, 8}, {32, 16}, {64, 4}, {16, 16}};
+const int kNumTileShapes = 4;
+
+bool tile_supported(int tx, int ty) {
+    for (int i = 0; i < kNumTileShapes; ++i)
+        if (kTileShapes[i].tx == tx && kTileShapes[i].ty == ty) return true;
+    return false;
+}
+
+static Consts to_consts(const his_solver_cfg* c) {
+    Consts k{};
+    k.g = c->g; k.h_dry = c->h_dry; k.kp_eps = c->kp_eps; k.cfl = c->cfl; k.dt_min = c->dt_min; k.dt_max = c->dt_max;
+    k.cfl_1d = c->cfl_1d; k.slot_width_frac = c->slot_width_frac; k.weir_cw = c->weir_cw;
+    k.exchange_limit = c->exchange_limit; k.exchange_relax = c->exchange_relax;
+    k.order = c->order; k.hllc = c->hllc;
+    return k;
+}
+
+static int bad(const std::string& msg) {
+    set_error(msg);
+    return HIS_ERR_BAD_ARG;
+}
+
+static int check_cfg(const his_solver_cfg* c) {
+    if (!c) return bad("cfg is NULL");
+    if (c->order != 1 && c->order != 2) return bad("order must be 1 or 2");
+    if (c->hllc != 0 && c->hllc != 1) return bad("hllc must be 0 or 1");
+    if (!(c->g > 0) || !(c->h_dry > 0) || !(c->kp_eps > 0)) return bad("g, h_dry and kp_eps must be positive");
+    return HIS_OK;
+}
+
+// CSR of `key` (values in [0, n)) listing positions in increasing order.
+static void build_csr(const int32_t* key, int len, int n, std::vector<int>& start, std::vector<int>& idx) {
+    start.assign(n + 1, 0);
+    for (int i = 0; i < len; ++i) start[key[i] + 1]++;
+    for (int i = 0; i < n; ++i) start[i + 1] += start[i];
+    idx.assign(len, 0);
+    std::vector<int> fill(start.begin(), start.end() - 1);
+    for (int i = 0; i < len; ++i) idx[fill[key[i]]++] = i;
+}
+
+// Device arena built from host vectors: returns offsets, one cudaMalloc, one copy.
+struct Arena {
+    std::vector<char> host;
+    size_t add(const void* p, size_t bytes) {
+        size_t off = (host.size() + 255) & ~size_t(255);
+        host.resize(off + bytes);
+        if (bytes) std::memcpy(host.data() + off, p, bytes);
+        return off;
+    }
+};
+
+}  // namespace his
+
+using namespace his;
+
+extern "C" {
+
+int32_t his_version(void) { return 100; }
+
+const char* his_last_error(void) { return g_last_error.c_str(); }
+
+// ------------------------------------------------------------------------- 2-D grid
+int32_t his_grid_create(int32_t precision, const his_solver_cfg* cfg, int32_t n_members, const his_grid_desc* grids,
+                        int32_t tile_x, int32_t tile_y, his_grid** out) {
+    if (!out) return bad("out is NULL");
+    *out = nullptr;
+    int rc = check_cfg(cfg);
+    if (rc) return rc;
+    if (precision != HIS_PREC_F64 && precision != HIS_PREC_F32) return bad("precision must be 0 (f64) or 1 (f32)");
+    if (n_members <= 0 || !grids) return bad("need at least one grid member");
+    if (tile_x == 0 && tile_y == 0) { tile_x = 32; tile_y = 8; }
+    if (!tile_supported(tile_x, tile_y)) return bad("unsupported tile shape");
+    for (int m = 0; m < n_members; ++m) {
+        const his_grid_desc& d = grids[m];
+        std::string who = "member " + std::to_string(m) + ": ";
+        if (d.ny <= 0 || d.nx <= 0) return bad(who + "grid must be at least 1 x 1");
+        if ((int64_t)d.ny * d.nx > (int64_t)1 << 30) return bad(who + "grid too large");
+        if (!(d.dx > 0) || !(d.dy > 0)) return bad(who + "dx and dy must be positive");
+        for (int e = 0; e < 4; ++e)
+            if (d.bc[e] < 0 || d.bc[e] > 3) return bad(who + "unknown boundary kind");
+        if (!d.h || !d.hu || !d.hv || !d.s_filled || !d.infil_cum || !d.z || !d.manning)
+            return bad(who + "state, bed and roughness pointers are required");
+        int nh = (d.f0 != nullptr) + (d.fc != nullptr) + (d.k != nullptr);
+        if (nh != 0 && nh != 3) return bad(who + "f0, fc and k must be given together");
+    }
+    his_grid* g = new his_grid();
+    g->prec = precision;
+    g->c = to_consts(cfg);
+    g->n = n_members;
+    g->tx = tile_x;
+    g->ty = tile_y;
+    g->desc.assign(grids, grids + n_members);
+    cudaGetDevice(&g->device);
+    rc = precision == HIS_PREC_F64 ? grid_init_f64(g) : grid_init_f32(g);
+    if (rc == HIS_OK) {
+        cudaError_t e = cudaMalloc(&g->d_params, sizeof(StepParams) * n_members);
+        if (e == cudaSuccess) e = cudaMemset(g->d_params, 0, sizeof(StepParams) * n_members);
+        if (e == cudaSuccess) e = cudaMalloc(&g->d_out, sizeof(double) * 8 * n_members);
+        if (e == cudaSuccess) e = cudaMemset(g->d_out, 0, sizeof(double) * 8 * n_members);
+        if (e == cudaSuccess) e = cudaMallocHost(&g->h_out, sizeof(double) * 8 * n_members);
+        if (e != cudaSuccess) rc = cuda_fail(e, "his_grid_create: allocation");
+    }
+    if (rc != HIS_OK) {
+        his_grid_destroy(g);
+        return rc;
+    }
+    *out = g;
+    return HIS_OK;
+}
+
+int32_t his_grid_destroy(his_grid* g) {
+    if (!g) return HIS_OK;
+    cudaFree(g->d_grids);
+    cudaFree(g->d_tiles);
+    cudaFree(g->d_params);
+    cudaFree(g->d_partials);
+    cudaFree(g->d_out);
+    cudaFree(g->d_scratch);
+    if (g->h_out) cudaFreeHost(g->h_out);
+    delete g;
+    return HIS_OK;
+}
+
+int64_t his_grid_scratch_bytes(const his_grid* g) {
+    return g ? (int64_t)(g->scratch_bytes + g->table_bytes) : 0;
+}
+
+static int upload_params(his_grid* g, const his_step_params* p, cudaStream_t s) {
+    std::vector<StepParams> sp(g->n);
+    for (int m = 0; m < g->n; ++m) {
+        const his_step_params& q = p[m];
+        if (!std::isfinite(q.dt) || !(q.dt >= 0) || !std::isfinite(q.t) || !std::isfinite(q.rain))
+            return bad("member " + std::to_string(m) + ": dt, t and rain must be finite (dt >= 0)");
+        sp[m].dt = q.dt; sp[m].t = q.t; sp[m].rain = q.rain;
+        for (int e = 0; e < 4; ++e) { sp[m].bc0[e] = q.bc_t[e]; sp[m].bc1[e] = q.bc_t_dt[e]; }
+        sp[m].active = 1;
+    }
+    // pageable source: returns once the data is staged, so `sp` may go out of scope
+    HIS_CK(cudaMemcpyAsync(g->d_params, sp.data(), sizeof(StepParams) * g->n, cudaMemcpyHostToDevice, s));
+    return HIS_OK;
+}
+
+static int fetch_out(his_grid* g, cudaStream_t s) {
+    HIS_CK(cudaMemcpyAsync(g->h_out, g->d_out, sizeof(double) * 8 * g->n, cudaMemcpyDeviceToHost, s));
+    HIS_CK(cudaStreamSynchronize(s));
+    return HIS_OK;
+}
+
+int32_t his_grid_step(his_grid* g, const his_step_params* params, double* vols, void* stream) {
+    if (!g || !params) return bad("grid and params are required");
+    cudaStream_t s = (cudaStream_t)stream;
+    int rc = upload_params(g, params, s);
+    if (rc) return rc;
+    rc = g->prec == HIS_PREC_F64 ? grid_step_f64(g, s) : grid_step_f32(g, s);
+    if (rc || !vols) return rc;
+    if ((rc = fetch_out(g, s))) return rc;
+    for (int m = 0; m < g->n; ++m)
+        for (int j = 0; j < 5; ++j) vols[m * 5 + j] = g->h_out[m * 8 + j];
+    return HIS_OK;
+}
+
+int32_t his_grid_max_rate(his_grid* g, double* rate, void* stream) {
+    if (!g || !rate) return bad("grid and rate are required");
+    cudaStream_t s = (cudaStream_t)stream;
+    int rc = g->prec == HIS_PREC_F64 ? grid_reduce_f64(g, s) : grid_reduce_f32(g, s);
+    if (rc || (rc = fetch_out(g, s))) return rc;
+    for (int m = 0; m < g->n; ++m) rate[m] = g->h_out[m * 8 + 5];
+    return HIS_OK;
+}
+
+int32_t his_grid_volumes(his_grid* g, double* vols, void* stream) {
+    if (!g || !vols) return bad("grid and vols are required");
+    cudaStream_t s = (cudaStream_t)stream;
+    int rc = g->prec == HIS_PREC_F64 ? grid_reduce_f64(g, s) : grid_reduce_f32(g, s);
+    if (rc || (rc = fetch_out(g, s))) return rc;
+    for (int m = 0; m < g->n; ++m) {
+        vols[m * 2 + 0] = g->h_out[m * 8 + 6];
+        vols[m * 2 + 1] = g->h_out[m * 8 + 7];
+    }
+    return HIS_OK;
+}
+
+// ------------------------------------------------------------------------ 1-D network
+int32_t his_net_create(const his_solver_cfg* cfg, int32_t n_members, const his_net_desc* nets, his_net** out) {
+    if (!out) return bad("out is NULL");
+    *out = nullptr;
+    int rc = check_cfg(cfg);
+    if (rc) return rc;
+    if (n_members <= 0 || !nets) return bad("need at least one network member");
+    Arena ar;
+    struct Offs { size_t kind, gsrc, fl, fr, gsign, ls, li, rs, ri, z, n, dx, b, m, yb, ts, fb, fm, fyb, fts; };
+    std::vector<Offs> offs(n_members);
+    size_t smem = 0;
+    for (int mb = 0; mb < n_members; ++mb) {
+        const his_net_desc& d = nets[mb];
+        std::string who = "network " + std::to_string(mb) + ": ";
+        if (d.n_cells <= 0 || d.n_faces <= 0) return bad(who + "needs cells and faces");
+        if (!d.kind || !d.ghost_src || !d.face_l || !d.face_r || !d.ghost_sign || !d.z || !d.manning || !d.dx ||
+            !d.b || !d.m || !d.yb || !d.ts || !d.fb || !d.fm || !d.fyb || !d.fts || !d.A || !d.Q)
+            return bad(who + "all arrays are required");
+        for (int i = 0; i < d.n_cells; ++i) {
+            if (d.kind[i] < 0 || d.kind[i] > 4) return bad(who + "cell kind out of range");
+            if (d.kind[i] >= 2 && (d.ghost_src[i] < 0 || d.ghost_src[i] >= d.n_cells))
+                return bad(who + "ghost cell without a valid interior neighbour");
+            if (!(d.dx[i] > 0) || !(d.b[i] > 0) || !(d.ts[i] > 0)) return bad(who + "dx, b and ts must be positive");
+        }
+        for (int f = 0; f < d.n_faces; ++f)
+            if (d.face_l[f] < 0 || d.face_l[f] >= d.n_cells || d.face_r[f] < 0 || d.face_r[f] >= d.n_cells)
+                return bad(who + "face cell index out of range");
+        std::vector<int> ls, li, rs, ri;
+        build_csr(d.face_l, d.n_faces, d.n_cells, ls, li);
+        build_csr(d.face_r, d.n_faces, d.n_cells, rs, ri);
+        std::vector<int32_t> gsrc(d.ghost_src, d.ghost_src + d.n_cells);
+        for (auto& x : gsrc) if (x < 0) x = 0;
+        Offs& o = offs[mb];
+        const size_t C = sizeof(double) * d.n_cells, F = sizeof(double) * d.n_faces;
+        o.kind = ar.add(d.kind, sizeof(int32_t) * d.n_cells);
+        o.gsrc = ar.add(gsrc.data(), sizeof(int32_t) * d.n_cells);
+        o.fl = ar.add(d.face_l, sizeof(int32_t) * d.n_faces);
+        o.fr = ar.add(d.face_r, sizeof(int32_t) * d.n_faces);
+        o.gsign = ar.add(d.ghost_sign, C);
+        o.ls = ar.add(ls.data(), sizeof(int) * ls.size());
+        o.li = ar.add(li.data(), sizeof(int) * li.size());
+        o.rs = ar.add(rs.data(), sizeof(int) * rs.size());
+        o.ri = ar.add(ri.data(), sizeof(int) * ri.size());
+        o.z = ar.add(d.z, C); o.n = ar.add(d.manning, C); o.dx = ar.add(d.dx, C);
+        o.b = ar.add(d.b, C); o.m = ar.add(d.m, C); o.yb = ar.add(d.yb, C); o.ts = ar.add(d.ts, C);
+        o.fb = ar.add(d.fb, F); o.fm = ar.add(d.fm, F); o.fyb = ar.add(d.fyb, F); o.fts = ar.add(d.fts, F);
+        smem = std::max(smem, net_smem_bytes(d.n_cells, d.n_faces));
+    }
+    if (smem > 200 * 1024) return bad("network too large for one thread block's shared memory");
+    his_net* N = new his_net();
+    N->c = to_consts(cfg);
+    N->n = n_members;
+    N->smem = smem;
+    N->max_sub = 256;
+    cudaGetDevice(&N->device);
+    auto fail = [&](cudaError_t e, const char* w) { int r = cuda_fail(e, w); his_net_destroy(N); return r; };
+    cudaError_t e = cudaMalloc(&N->d_arena, ar.host.size() ? ar.host.size() : 256);
+    if (e != cudaSuccess) return fail(e, "his_net_create: arena");
+    N->arena_bytes = ar.host.size();
+    e = cudaMemcpy(N->d_arena, ar.host.data(), ar.host.size(), cudaMemcpyHostToDevice);
+    if (e != cudaSuccess) return fail(e, "his_net_create: copy");
+    char* base = (char*)N->d_arena;
+    N->h_nets.resize(n_members);
+    for (int mb = 0; mb < n_members; ++mb) {
+        const his_net_desc& d = nets[mb];
+        const Offs& o = offs[mb];
+        Net& n = N->h_nets[mb];
+        n.n_cells = d.n_cells; n.n_faces = d.n_faces;
+        n.kind = (const int*)(base + o.kind); n.gsrc = (const int*)(base + o.gsrc);
+        n.fl = (const int*)(base + o.fl); n.fr = (const int*)(base + o.fr);
+        n.gsign = (const double*)(base + o.gsign);
+        n.lstart = (const int*)(base + o.ls); n.lidx = (const int*)(base + o.li);
+        n.rstart = (const int*)(base + o.rs); n.ridx = (const int*)(base + o.ri);
+        n.z = (const double*)(base + o.z); n.nman = (const double*)(base + o.n); n.dx = (const double*)(base + o.dx);
+        n.b = (const double*)(base + o.b); n.m = (const double*)(base + o.m);
+        n.yb = (const double*)(base + o.yb); n.ts = (const double*)(base + o.ts);
+        n.fb = (const double*)(base + o.fb); n.fm = (const double*)(base + o.fm);
+        n.fyb = (const double*)(base + o.fyb); n.fts = (const double*)(base + o.fts);
+        n.A = d.A; n.Q = d.Q;
+    }
+    e = cudaMalloc(&N->d_nets, sizeof(Net) * n_members);
+    if (e == cudaSuccess) e = cudaMemcpy(N->d_nets, N->h_nets.data(), sizeof(Net) * n_members, cudaMemcpyHostToDevice);
+    if (e == cudaSuccess) e = cudaMalloc(&N->d_forcing, sizeof(double) * 2 * N->max_sub * n_members);
+    if (e == cudaSuccess) e = cudaMalloc(&N->d_out, sizeof(double) * 3 * n_members);
+    if (e == cudaSuccess) e = cudaMallocHost(&N->h_out, sizeof(double) * 3 * n_members);
+    if (e != cudaSuccess) return fail(e, "his_net_create: allocation");
+    *out = N;
+    return HIS_OK;
+}
+
+int32_t his_net_destroy(his_net* N) {
+    if (!N) return HIS_OK;
+    cudaFree(N->d_arena);
+    cudaFree(N->d_nets);
+    cudaFree(N->d_forcing);
+    cudaFree(N->d_out);
+    if (N->h_out) cudaFreeHost(N->h_out);
+    delete N;
+    return HIS_OK;
+}
+
+int32_t his_net_step(his_net* N, double dt, int32_t n_sub, const double* forcing, double* vols, void* stream) {
+    if (!N || !forcing) return bad("network and forcing are required");
+    if (n_sub < 1 || n_sub > N->max_sub) return bad("n_sub must be in [1, 256]");
+    if (!std::isfinite(dt) || !(dt >= 0)) return bad("dt must be finite and >= 0");
+    cudaStream_t s = (cudaStream_t)stream;
+    HIS_CK(cudaMemcpyAsync(N->d_forcing, forcing, sizeof(double) * 2 * n_sub * N->n, cudaMemcpyHostToDevice, s));
+    int rc = net_step_launch(N, dt, n_sub, s);
+    if (rc || !vols) return rc;
+    HIS_CK(cudaMemcpyAsync(N->h_out, N->d_out, sizeof(double) * 3 * N->n, cudaMemcpyDeviceToHost, s));
+    HIS_CK(cudaStreamSynchronize(s));
+    std::memcpy(vols, N->h_out, sizeof(double) * 3 * N->n);
+    return HIS_OK;
+}
+
+static int net_reduce(his_net* N, cudaStream_t s) {
+    int rc = net_reduce_launch(N, s);
+    if (rc) return rc;
+    HIS_CK(cudaMemcpyAsync(N->h_out, N->d_out, sizeof(double) * 3 * N->n, cudaMemcpyDeviceToHost, s));
+    HIS_CK(cudaStreamSynchronize(s));
+    return HIS_OK;
+}
+
+int32_t his_net_max_rate(his_net* N, double* rate, int32_t* any_wet, void* stream) {
+    if (!N || !rate || !any_wet) return bad("network, rate and any_wet are required");
+    int rc = net_reduce(N, (cudaStream_t)stream);
+    if (rc) return rc;
+    for (int m = 0; m < N->n; ++m) {
+        rate[m] = N->h_out[m * 3 + 0];
+        any_wet[m] = N->h_out[m * 3 + 1] > 0.0 ? 1 : 0;
+    }
+    return HIS_OK;
+}
+
+int32_t his_net_volume(his_net* N, double* vol, void* stream) {
+    if (!N || !vol) return bad("network and vol are required");
+    int rc = net_reduce(N, (cudaStream_t)stream);
+    if (rc) return rc;
+    for (int m = 0; m < N->n; ++m) vol[m] = N->h_out[m * 3 + 2];
+    return HIS_OK;
+}
+
+// ---------------------------------------------------------------------------- links
+int32_t his_links_create(his_grid* grid, his_net* net, int32_t n_members, const his_links_desc* links,
+                         his_links** out) {
+    if (!out) return bad("out is NULL");
+    *out = nullptr;
+    if (!grid || !net || !links) return bad("grid, net and links are required");
+    if (n_members != grid->n || n_members != net->n)
+        return bad("links, grid and network must have the same number of members");
+    Arena ar;
+    struct Offs { size_t c1, inv, uq, zb, len, z2, us, ui, cs, ci; };
+    std::vector<Offs> offs(n_members);
+    size_t smem = 0;
+    int total = 0;
+    for (int mb = 0; mb < n_members; ++mb) {
+        const his_links_desc& d = links[mb];
+        const his_grid_desc& gd = grid->desc[mb];
+        const int nc = net->h_nets[mb].n_cells;
+        std::string who = "links " + std::to_string(mb) + ": ";
+        if (d.n_links < 0 || d.n_unique < 0) return bad(who + "negative count");
+        if (d.n_links > 0 && (!d.cell1d || !d.inv || !d.uniq || !d.zbank || !d.length || !d.z2))
+            return bad(who + "all arrays are required");
+        std::vector<int32_t> uq(d.n_unique);
+        for (int k = 0; k < d.n_unique; ++k) {
+            if (d.uniq[k] < 0 || d.uniq[k] >= (int64_t)gd.ny * gd.nx) return bad(who + "2-D cell index out of range");
+            uq[k] = (int32_t)d.uniq[k];
+        }
+        for (int l = 0; l < d.n_links; ++l) {
+            if (d.cell1d[l] < 0 || d.cell1d[l] >= nc) return bad(who + "1-D cell index out of range");
+            if (d.inv[l] < 0 || d.inv[l] >= d.n_unique) return bad(who + "unique index out of range");
+        }
+        std::vector<int> us, ui, cs, ci;
+        build_csr(d.inv, d.n_links, d.n_unique, us, ui);
+        build_csr(d.cell1d, d.n_links, nc, cs, ci);
+        Offs& o = offs[mb];
+        const size_t L = sizeof(double) * d.n_links;
+        o.c1 = ar.add(d.cell1d, sizeof(int32_t) * d.n_links);
+        o.inv = ar.add(d.inv, sizeof(int32_t) * d.n_links);
+        o.uq = ar.add(uq.data(), sizeof(int32_t) * uq.size());
+        o.zb = ar.add(d.zbank, L); o.len = ar.add(d.length, L); o.z2 = ar.add(d.z2, L);
+        o.us = ar.add(us.data(), sizeof(int) * us.size()); o.ui = ar.add(ui.data(), sizeof(int) * ui.size());
+        o.cs = ar.add(cs.data(), sizeof(int) * cs.size()); o.ci = ar.add(ci.data(), sizeof(int) * ci.size());
+        smem = std::max(smem, exchange_smem_bytes(d.n_links, d.n_unique, nc));
+        total += d.n_links;
+    }
+    if (smem > 200 * 1024) return bad("too many links for one thread block's shared memory");
+    his_links* Lk = new his_links();
+    Lk->grid = grid; Lk->net = net; Lk->n = n_members; Lk->total_links = total; Lk->smem = smem;
+    auto fail = [&](cudaError_t e, const char* w) { int r = cuda_fail(e, w); his_links_destroy(Lk); return r; };
+    cudaError_t e = cudaMalloc(&Lk->d_arena, ar.host.size() ? ar.host.size() : 256);
+    if (e == cudaSuccess) e = cudaMemcpy(Lk->d_arena, ar.host.data(), ar.host.size(), cudaMemcpyHostToDevice);
+    if (e != cudaSuccess) return fail(e, "his_links_create: arena");
+    char* base = (char*)Lk->d_arena;
+    std::vector<Lnk> H(n_members);
+    int voff = 0;
+    for (int mb = 0; mb < n_members; ++mb) {
+        const his_links_desc& d = links[mb];
+        const Offs& o = offs[mb];
+        Lnk& L = H[mb];
+        L.n_links = d.n_links; L.n_unique = d.n_unique; L.v_offset = voff;
+        voff += d.n_links;
+        L.cell1d = (const int*)(base + o.c1); L.inv = (const int*)(base + o.inv); L.uniq = (const int*)(base + o.uq);
+        L.zbank = (const double*)(base + o.zb); L.length = (const double*)(base + o.len);
+        L.z2 = (const double*)(base + o.z2);
+        L.ustart = (const int*)(base + o.us); L.uidx = (const int*)(base + o.ui);
+        L.cstart = (const int*)(base + o.cs); L.cidx = (const int*)(base + o.ci);
+    }
+    e = cudaMalloc(&Lk->d_links, sizeof(Lnk) * n_members);
+    if (e == cudaSuccess) e = cudaMemcpy(Lk->d_links, H.data(), sizeof(Lnk) * n_members, cudaMemcpyHostToDevice);
+    if (e == cudaSuccess) e = cudaMalloc(&Lk->d_V, sizeof(double) * std::max(total, 1));
+    if (e == cudaSuccess) e = cudaMallocHost(&Lk->h_V, sizeof(double) * std::max(total, 2 * n_members));
+    if (e == cudaSuccess) e = cudaMalloc(&Lk->d_exch, sizeof(double) * 2 * n_members);
+    if (e == cudaSuccess) e = cudaMemset(Lk->d_exch, 0, sizeof(double) * 2 * n_members);
+    if (e != cudaSuccess) return fail(e, "his_links_create: allocation");
+    *out = Lk;
+    return HIS_OK;
+}
+
+int32_t his_links_destroy(his_links* L) {
+    if (!L) return HIS_OK;
+    cudaFree(L->d_arena);
+    cudaFree(L->d_links);
+    cudaFree(L->d_V);
+    cudaFree(L->d_exch);
+    if (L->h_V) cudaFreeHost(L->h_V);
+    delete L;
+    return HIS_OK;
+}
+
+int32_t his_exchange(his_links* L, const his_solver_cfg* cfg, double dt, double* V, void* stream) {
+    if (!L) return bad("links are required");
+    if (!std::isfinite(dt) || !(dt >= 0)) return bad("dt must be finite and >= 0");
+    Consts c = L->grid->c;
+    if (cfg) {
+        c.weir_cw = cfg->weir_cw;
+        c.exchange_limit = cfg->exchange_limit;
+        c.exchange_relax = cfg->exchange_relax;
+    }
+    cudaStream_t s = (cudaStream_t)stream;
+    int rc = L->grid->prec == HIS_PREC_F64 ? exchange_f64(L, c, dt, s) : exchange_f32(L, c, dt, s);
+    if (rc || !V) return rc;
+    HIS_CK(cudaMemcpyAsync(L->h_V, L->d_V, sizeof(double) * std::max(L->total_links, 1), cudaMemcpyDeviceToHost, s));
+    HIS_CK(cudaStreamSynchronize(s));
+    std::memcpy(V, L->h_V, sizeof(double) * L->total_links);
+    return HIS_OK;
+}
+
+int32_t his_links_exchanged(his_links* L, double* totals, int32_t reset, void* stream) {
+    if (!L || !totals) return bad("links and totals are required");
+    cudaStream_t s = (cudaStream_t)stream;
+    HIS_CK(cudaMemcpyAsync(L->h_V, L->d_exch, sizeof(double) * 2 * L->n, cudaMemcpyDeviceToHost, s));
+    HIS_CK(cudaStreamSynchronize(s));
+    std::memcpy(totals, L->h_V, sizeof(double) * 2 * L->n);
+    if (reset) HIS_CK(cudaMemsetAsync(L->d_exch, 0, sizeof(double) * 2 * L->n, s));
+    return HIS_OK;
+}
+
+}  // extern "C"

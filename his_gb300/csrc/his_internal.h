@@ -1,0 +1,88 @@
+// Host-side state behind the opaque handles of his_gb300.h (not part of the ABI).
+#pragma once
+#include <cstdint>
+#include <string>
+#include <vector>
+
+#include <cuda_runtime.h>
+
+#include "his_device.cuh"
+#include "net1d_kernels.cuh"
+
+struct his_grid {
+    int prec = 0;
+    his::Consts c{};
+    int n = 0, tx = 32, ty = 8, device = 0;
+    std::vector<his_grid_desc> desc;
+    std::vector<int> tile0, ntile;
+    void* d_grids = nullptr;                 // his::Grid<R>[n]
+    his::TileRef* d_tiles = nullptr;
+    int n_tiles = 0;
+    his::StepParams* d_params = nullptr;
+    double* d_partials = nullptr;            // n_tiles x NPART
+    double* d_out = nullptr;                 // n x 8
+    double* h_out = nullptr;                 // pinned mirror of d_out
+    void* d_scratch = nullptr;               // stage buffers of every member
+    size_t scratch_bytes = 0;
+    size_t table_bytes = 0;
+};
+
+struct his_net {
+    his::Consts c{};
+    int n = 0, device = 0;
+    std::vector<his::Net> h_nets;
+    his::Net* d_nets = nullptr;
+    void* d_arena = nullptr;
+    size_t arena_bytes = 0;
+    double* d_forcing = nullptr;
+    int max_sub = 0;
+    double* d_out = nullptr;                 // n x 3
+    double* h_out = nullptr;
+    size_t smem = 0;
+};
+
+struct his_links {
+    his_grid* grid = nullptr;
+    his_net* net = nullptr;
+    int n = 0, total_links = 0;
+    his::Lnk* d_links = nullptr;
+    void* d_arena = nullptr;
+    double* d_V = nullptr;
+    double* h_V = nullptr;
+    double* d_exch = nullptr;                // n x 2 running exchange totals
+    size_t smem = 0;
+};
+
+namespace his {
+
+void set_error(const std::string& msg);
+int cuda_fail(cudaError_t e, const char* what);
+
+#define HIS_CK(call)                                          \
+    do {                                                      \
+        cudaError_t e_ = (call);                              \
+        if (e_ != cudaSuccess) return his::cuda_fail(e_, #call); \
+    } while (0)
+
+// Tile shapes compiled into the library (TX, TY)
+struct TileShape { int tx, ty; };
+extern const TileShape kTileShapes[];
+extern const int kNumTileShapes;
+bool tile_supported(int tx, int ty);
+
+// precision-specific entry points (swe2d_f64.cu / swe2d_f32.cu)
+int grid_init_f64(his_grid* g);
+int grid_init_f32(his_grid* g);
+int grid_step_f64(his_grid* g, cudaStream_t s);
+int grid_step_f32(his_grid* g, cudaStream_t s);
+int grid_reduce_f64(his_grid* g, cudaStream_t s);
+int grid_reduce_f32(his_grid* g, cudaStream_t s);
+int exchange_f64(his_links* l, const Consts& c, double dt, cudaStream_t s);
+int exchange_f32(his_links* l, const Consts& c, double dt, cudaStream_t s);
+size_t stage_smem_bytes(int prec, int tx, int ty);
+
+// net1d.cu
+int net_step_launch(his_net* n, double dt, int n_sub, cudaStream_t s);
+int net_reduce_launch(his_net* n, cudaStream_t s);
+
+}  // namespace his

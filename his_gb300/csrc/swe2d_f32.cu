@@ -1,0 +1,13 @@
+// Production form: 2-D state, fluxes and updates in float32 (float64 volume sums and
+// exchange volumes).  Built with fused multiply-add enabled.
+#include "swe2d_impl.cuh"
+
+namespace his {
+int grid_init_f32(his_grid* g) { return grid_init_impl<float>(g); }
+int grid_step_f32(his_grid* g, cudaStream_t s) { return grid_step_impl<float>(g, s); }
+int grid_reduce_f32(his_grid* g, cudaStream_t s) { return grid_reduce_impl<float>(g, s); }
+int exchange_f32(his_links* l, const Consts& c, double dt, cudaStream_t s) { return exchange_impl<float>(l, c, dt, s); }
+size_t stage_smem_bytes(int prec, int tx, int ty) {
+    return prec == HIS_PREC_F64 ? stage_smem_impl<double>(tx, ty) : stage_smem_impl<float>(tx, ty);
+}
+}  // namespace his

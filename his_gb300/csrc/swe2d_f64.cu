@@ -1,0 +1,10 @@
+// Plain method: every 2-D kernel instantiated in float64.  Built with -fmad=false so
+// products and sums round separately, as in the reference's float64 torch ops.
+#include "swe2d_impl.cuh"
+
+namespace his {
+int grid_init_f64(his_grid* g) { return grid_init_impl<double>(g); }
+int grid_step_f64(his_grid* g, cudaStream_t s) { return grid_step_impl<double>(g, s); }
+int grid_reduce_f64(his_grid* g, cudaStream_t s) { return grid_reduce_impl<double>(g, s); }
+int exchange_f64(his_links* l, const Consts& c, double dt, cudaStream_t s) { return exchange_impl<double>(l, c, dt, s); }
+}  // namespace his

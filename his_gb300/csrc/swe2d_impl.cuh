@@ -1,0 +1,149 @@
+// Precision-templated host launchers of the 2-D kernels and the weir exchange.
+// Included once per precision by swe2d_f64.cu and swe2d_f32.cu.
+#pragma once
+#include <vector>
+
+#include "his_internal.h"
+#include "net1d_kernels.cuh"
+#include "swe2d_kernels.cuh"
+
+namespace his {
+
+template <class R, int TX, int TY>
+int set_tile_attrs() {
+    using G = TileGeom<R, TX, TY>;
+    const int bytes = (int)G::smem_bytes;
+    HIS_CK(cudaFuncSetAttribute(stage_kernel<R, TX, TY, 0>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes));
+    HIS_CK(cudaFuncSetAttribute(stage_kernel<R, TX, TY, 1>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes));
+    HIS_CK(cudaFuncSetAttribute(stage_kernel<R, TX, TY, 2>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes));
+    return HIS_OK;
+}
+
+template <class R, int TX, int TY>
+int launch_step_shape(his_grid* g, cudaStream_t s) {
+    using G = TileGeom<R, TX, TY>;
+    auto* grids = reinterpret_cast<const Grid<R>*>(g->d_grids);
+    if (g->c.order == 2) {
+        stage_kernel<R, TX, TY, 1><<<g->n_tiles, G::NT, G::smem_bytes, s>>>(grids, g->d_tiles, g->d_params, g->c,
+                                                                            g->d_partials);
+        stage_kernel<R, TX, TY, 2><<<g->n_tiles, G::NT, G::smem_bytes, s>>>(grids, g->d_tiles, g->d_params, g->c,
+                                                                            g->d_partials);
+    } else {
+        stage_kernel<R, TX, TY, 0><<<g->n_tiles, G::NT, G::smem_bytes, s>>>(grids, g->d_tiles, g->d_params, g->c,
+                                                                            g->d_partials);
+    }
+    finalize_kernel<R><<<g->n, 32, 0, s>>>(grids, g->d_params, g->c, g->d_partials, g->d_out, 0);
+    HIS_CK(cudaGetLastError());
+    return HIS_OK;
+}
+
+template <class R, int TX, int TY>
+int launch_reduce_shape(his_grid* g, cudaStream_t s) {
+    auto* grids = reinterpret_cast<const Grid<R>*>(g->d_grids);
+    cell_reduce_kernel<R, TX, TY><<<g->n_tiles, TX * TY, 0, s>>>(grids, g->d_tiles, g->c, g->d_partials);
+    finalize_kernel<R><<<g->n, 32, 0, s>>>(grids, g->d_params, g->c, g->d_partials, g->d_out, 1);
+    HIS_CK(cudaGetLastError());
+    return HIS_OK;
+}
+
+#define HIS_TILE_DISPATCH(FN, R, g, ...)                                      \
+    do {                                                                      \
+        if (g->tx == 32 && g->ty == 8) return FN<R, 32, 8>(g, __VA_ARGS__);   \
+        if (g->tx == 32 && g->ty == 16) return FN<R, 32, 16>(g, __VA_ARGS__); \
+        if (g->tx == 64 && g->ty == 4) return FN<R, 64, 4>(g, __VA_ARGS__);   \
+        if (g->tx == 16 && g->ty == 16) return FN<R, 16, 16>(g, __VA_ARGS__); \
+        set_error("unsupported tile shape");                                  \
+        return HIS_ERR_BAD_ARG;                                               \
+    } while (0)
+
+template <class R>
+int grid_init_impl(his_grid* g) {
+    int rc;
+    if ((rc = set_tile_attrs<R, 32, 8>()) != HIS_OK) return rc;
+    if ((rc = set_tile_attrs<R, 32, 16>()) != HIS_OK) return rc;
+    if ((rc = set_tile_attrs<R, 64, 4>()) != HIS_OK) return rc;
+    if ((rc = set_tile_attrs<R, 16, 16>()) != HIS_OK) return rc;
+    const int n = g->n;
+    std::vector<Grid<R>> H(n);
+    std::vector<TileRef> tiles;
+    g->tile0.assign(n, 0);
+    g->ntile.assign(n, 0);
+    // stage buffers: three planes per member, each 256-byte aligned
+    std::vector<size_t> off(n);
+    size_t total = 0;
+    for (int m = 0; m < n; ++m) {
+        const his_grid_desc& d = g->desc[m];
+        size_t plane = ((size_t)d.ny * d.nx * sizeof(R) + 255) & ~size_t(255);
+        off[m] = total;
+        total += 3 * plane;
+    }
+    g->scratch_bytes = total;
+    HIS_CK(cudaMalloc(&g->d_scratch, total > 0 ? total : 256));
+    for (int m = 0; m < n; ++m) {
+        const his_grid_desc& d = g->desc[m];
+        Grid<R>& G = H[m];
+        G.ny = d.ny;
+        G.nx = d.nx;
+        for (int e = 0; e < 4; ++e) G.bc[e] = d.bc[e];
+        G.dx = d.dx;
+        G.dy = d.dy;
+        G.area = d.dx * d.dy;
+        G.t0 = d.horton_t0;
+        G.tiles_x = (d.nx + g->tx - 1) / g->tx;
+        G.tiles_y = (d.ny + g->ty - 1) / g->ty;
+        G.n_tiles = G.tiles_x * G.tiles_y;
+        G.tile0 = (int)tiles.size();
+        g->tile0[m] = G.tile0;
+        g->ntile[m] = G.n_tiles;
+        for (int ty = 0; ty < G.tiles_y; ++ty)
+            for (int tx = 0; tx < G.tiles_x; ++tx)
+                tiles.push_back(TileRef{m, tx * g->tx, ty * g->ty, ty * G.tiles_x + tx});
+        G.h = (R*)d.h; G.hu = (R*)d.hu; G.hv = (R*)d.hv; G.sf = (R*)d.s_filled; G.ic = (R*)d.infil_cum;
+        size_t plane = ((size_t)d.ny * d.nx * sizeof(R) + 255) & ~size_t(255);
+        char* base = (char*)g->d_scratch + off[m];
+        G.h1 = (R*)base; G.hu1 = (R*)(base + plane); G.hv1 = (R*)(base + 2 * plane);
+        G.z = (const R*)d.z; G.n = (const R*)d.manning; G.S = (const R*)d.storage;
+        G.f0 = (const R*)d.f0; G.fc = (const R*)d.fc; G.k = (const R*)d.k; G.rw = (const R*)d.rain_weight;
+    }
+    g->n_tiles = (int)tiles.size();
+    HIS_CK(cudaMalloc(&g->d_grids, sizeof(Grid<R>) * n));
+    HIS_CK(cudaMemcpy(g->d_grids, H.data(), sizeof(Grid<R>) * n, cudaMemcpyHostToDevice));
+    HIS_CK(cudaMalloc(&g->d_tiles, sizeof(TileRef) * tiles.size()));
+    HIS_CK(cudaMemcpy(g->d_tiles, tiles.data(), sizeof(TileRef) * tiles.size(), cudaMemcpyHostToDevice));
+    HIS_CK(cudaMalloc(&g->d_partials, sizeof(double) * NPART * (size_t)g->n_tiles));
+    HIS_CK(cudaMemset(g->d_partials, 0, sizeof(double) * NPART * (size_t)g->n_tiles));
+    g->table_bytes = sizeof(Grid<R>) * n + sizeof(TileRef) * tiles.size() + sizeof(double) * NPART * g->n_tiles;
+    return HIS_OK;
+}
+
+template <class R>
+int grid_step_impl(his_grid* g, cudaStream_t s) {
+    HIS_TILE_DISPATCH(launch_step_shape, R, g, s);
+}
+
+template <class R>
+int grid_reduce_impl(his_grid* g, cudaStream_t s) {
+    HIS_TILE_DISPATCH(launch_reduce_shape, R, g, s);
+}
+
+template <class R>
+int exchange_impl(his_links* l, const Consts& c, double dt, cudaStream_t s) {
+    if (l->smem > 48 * 1024)
+        HIS_CK(cudaFuncSetAttribute(exchange_kernel<R>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)l->smem));
+    exchange_kernel<R><<<l->n, 256, l->smem, s>>>(l->d_links, l->net->d_nets,
+                                                  reinterpret_cast<const Grid<R>*>(l->grid->d_grids), nullptr, c,
+                                                  dt, l->d_V, l->d_exch);
+    HIS_CK(cudaGetLastError());
+    return HIS_OK;
+}
+
+template <class R>
+size_t stage_smem_impl(int tx, int ty) {
+    if (tx == 32 && ty == 8) return TileGeom<R, 32, 8>::smem_bytes;
+    if (tx == 32 && ty == 16) return TileGeom<R, 32, 16>::smem_bytes;
+    if (tx == 64 && ty == 4) return TileGeom<R, 64, 4>::smem_bytes;
+    if (tx == 16 && ty == 16) return TileGeom<R, 16, 16>::smem_bytes;
+    return 0;
+}
+
+}  // namespace his

@@ -1,0 +1,167 @@
+/*
+ * his_gb300.h -- C ABI of the GB300-native flood-engine time step.
+ *
+ * Plain C: opaque handles, plain pointers and sizes, int status codes.  Device
+ * pointers are CUDA device addresses (e.g. torch tensors' data_ptr()); "host"
+ * arrays are ordinary host memory copied by the call.  `stream` is a
+ * cudaStream_t passed as void* (0 = legacy default stream).  Every call is
+ * asynchronous on `stream` unless it returns host results, in which case it
+ * synchronises that stream before returning.
+ *
+ * Each entry point cites the reference interface it replaces (file:line in the
+ * reference project hydrointel, Elciiid/HIS).
+ */
+#ifndef HIS_GB300_H
+#define HIS_GB300_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---------------------------------------------------------------- status codes */
+#define HIS_OK 0
+#define HIS_ERR_BAD_ARG 1        /* shape/count mismatch, bad kind, null pointer -> Python ValueError   */
+#define HIS_ERR_NONFINITE 2      /* a member's state went non-finite -> NumericalInstabilityError       */
+#define HIS_ERR_IMPLAUSIBLE 3    /* a member's state is physically impossible -> NumericalInstabilityError */
+#define HIS_ERR_WAIT_TIMEOUT 4   /* a bounded device wait gave up                                        */
+#define HIS_ERR_OOM_ADMISSION 5  /* request does not fit the HBM budget                                  */
+#define HIS_ERR_CUDA 6           /* CUDA runtime error (message via his_last_error)                      */
+#define HIS_ERR_UNSUPPORTED 7    /* feature not available in this build                                  */
+
+#define HIS_PREC_F64 0           /* plain method: all arithmetic float64                                  */
+#define HIS_PREC_F32 1           /* production form: float32 state and fluxes, float64 accumulators      */
+
+/* Edge order of bc[] and boundary values: west, east, south, north (row 0 = south).
+ * Kinds: 0 closed, 1 transmissive, 2 stage, 3 discharge.
+ * Replaces: hydrointel/solver/boundaries.py:25-46 (EDGES, EdgeBC, edge_values). */
+
+/* Solver constants.  Replaces hydrointel/config.py:96-131 (SolverConfig). */
+typedef struct his_solver_cfg {
+    double g, h_dry, kp_eps, cfl, dt_min, dt_max;
+    double cfl_1d, slot_width_frac, weir_cw, exchange_limit, exchange_relax;
+    int32_t order;   /* 1 or 2 (MUSCL + SSP-RK2) */
+    int32_t hllc;    /* 1 HLLC, 0 HLL */
+} his_solver_cfg;
+
+/* One member of a 2-D grid set: its own grid size, spacing, edges and fields.
+ * All pointers are device pointers of the set's precision (double* or float*),
+ * row-major (ny, nx).  Fields may alias between members (a shared bed).
+ * storage, f0/fc/k and rain_weight may be NULL (feature off).
+ * Replaces the state and fields of hydrointel/solver/swe2d.py:114-146 (SWE2D.__init__). */
+typedef struct his_grid_desc {
+    int32_t ny, nx;
+    int32_t bc[4];
+    double dx, dy;
+    double horton_t0;
+    void *h, *hu, *hv, *s_filled, *infil_cum;
+    const void *z, *manning, *storage, *f0, *fc, *k, *rain_weight;
+} his_grid_desc;
+
+/* Per-member forcing of one step: dt, step-start time, rain rate (m/s) and edge
+ * values at t and t+dt.  Replaces the packed per-member step quantities of
+ * hydrointel/solver/swe2d.py:282-303 (SWE2D._pack / step). */
+typedef struct his_step_params {
+    double dt, t, rain;
+    double bc_t[4], bc_t_dt[4];
+} his_step_params;
+
+typedef struct his_grid his_grid;
+typedef struct his_net his_net;
+typedef struct his_links his_links;
+
+/* Library version and the message of the last failing call on this thread. */
+int32_t his_version(void);
+const char* his_last_error(void);
+
+/* Create a set of n_members 2-D grids computed in `precision`.  tile_x/tile_y pick
+ * the stencil tile (0, 0 = default); the set allocates its own stage scratch.
+ * Replaces hydrointel/solver/swe2d.py:113-146 (SWE2D constructor, batched form). */
+int32_t his_grid_create(int32_t precision, const his_solver_cfg* cfg, int32_t n_members, const his_grid_desc* grids,
+                        int32_t tile_x, int32_t tile_y, his_grid** out);
+int32_t his_grid_destroy(his_grid* grid);
+
+/* Bytes of device scratch the set allocated (stage buffers, partials, tables). */
+int64_t his_grid_scratch_bytes(const his_grid* grid);
+
+/* Advance every member by one SSP-RK2 step with its own params (host array of
+ * n_members).  If vols is non-NULL it receives n_members x 5 float64 volumes
+ * (bnd_in, bnd_out, rain, infil, clip; m^3) and the call synchronises `stream`.
+ * Replaces hydrointel/solver/swe2d.py:298-371 (SWE2D.step / _step_core). */
+int32_t his_grid_step(his_grid* grid, const his_step_params* params, double* vols, void* stream);
+
+/* Per-member CFL rate max over wet cells of (|u|+c)/dx + (|v|+c)/dy (host out,
+ * n_members values; synchronises).  Replaces hydrointel/solver/swe2d.py:179-193
+ * (SWE2D._max_rate / max_dt, which reduces over the batch as well). */
+int32_t his_grid_max_rate(his_grid* grid, double* rate, void* stream);
+
+/* Per-member surface and retained volumes sum(h)*area, sum(s_filled)*area (host out,
+ * n_members x 2; synchronises).  Replaces hydrointel/solver/swe2d.py:169-174. */
+int32_t his_grid_volumes(his_grid* grid, double* vols, void* stream);
+
+/* One member's 1-D channel network (flattened cells and faces; kinds 0 reach,
+ * 1 junction, 2 inflow ghost, 3 stage ghost, 4 closed ghost).  Arrays are HOST
+ * arrays copied at creation; A and Q are DEVICE float64 state (n_cells each).
+ * Replaces hydrointel/solver/swe1d.py:113-166, :176-231 (Topology, SWE1D.__init__). */
+typedef struct his_net_desc {
+    int32_t n_cells, n_faces;
+    const int32_t *kind, *ghost_src, *face_l, *face_r;
+    const double* ghost_sign;
+    const double *z, *manning, *dx;
+    const double *b, *m, *yb, *ts;        /* cell sections */
+    const double *fb, *fm, *fyb, *fts;    /* face sections */
+    double *A, *Q;
+} his_net_desc;
+
+int32_t his_net_create(const his_solver_cfg* cfg, int32_t n_members, const his_net_desc* nets, his_net** out);
+int32_t his_net_destroy(his_net* net);
+
+/* n_sub 1-D substeps of dt/n_sub each for every member.  forcing: host array
+ * n_members x n_sub x 2 (inflow m^3/s, stage m) at the substep start times.  If vols
+ * is non-NULL it receives n_members x 3 float64 (bnd_in, bnd_out, clip) summed over
+ * the substeps and the call synchronises.
+ * Replaces hydrointel/solver/swe1d.py:265-368 (SWE1D._fill_ghosts / step / _step_core)
+ * and the substep loop of hydrointel/solver/coupling.py:216-221. */
+int32_t his_net_step(his_net* net, double dt, int32_t n_sub, const double* forcing, double* vols, void* stream);
+
+/* Per-member 1-D CFL rate max over wet interior cells of (|u| + sqrt(gA/T))/dx and
+ * whether any cell is wet (host outs; synchronises).
+ * Replaces hydrointel/solver/swe1d.py:253-262 (SWE1D.max_dt). */
+int32_t his_net_max_rate(his_net* net, double* rate, int32_t* any_wet, void* stream);
+
+/* Per-member channel volume sum(A*dx) over interior cells (host out; synchronises).
+ * Replaces hydrointel/solver/swe1d.py:245-247 (SWE1D.volume). */
+int32_t his_net_volume(his_net* net, double* vol, void* stream);
+
+/* Weir links between a grid set and a network set (member i of each).  HOST arrays,
+ * per member, copied at creation: cell1d, inv (-> unique cell), uniq (flat 2-D index
+ * of each unique linked cell), zbank, length, z2.
+ * Replaces hydrointel/solver/coupling.py:47-70 (Links, build_links). */
+typedef struct his_links_desc {
+    int32_t n_links, n_unique;
+    const int32_t *cell1d, *inv;
+    const int64_t* uniq;
+    const double *zbank, *length, *z2;
+} his_links_desc;
+
+int32_t his_links_create(his_grid* grid, his_net* net, int32_t n_members, const his_links_desc* links,
+                         his_links** out);
+int32_t his_links_destroy(his_links* links);
+
+/* Villemonte weir exchange for every member, applied in place to the 2-D depth and
+ * momenta and the 1-D area.  cfg supplies weir_cw, exchange_limit and
+ * exchange_relax for this call (NULL = the grid set's constants).  If V is non-NULL
+ * it receives the per-link volumes (members concatenated, + = 2-D -> 1-D) and the
+ * call synchronises.  Replaces hydrointel/solver/coupling.py:73-124 (exchange). */
+int32_t his_exchange(his_links* links, const his_solver_cfg* cfg, double dt, double* V, void* stream);
+
+/* Running per-member totals of exchanged volume since creation or the last reset:
+ * n_members x 2 (2-D -> 1-D, 1-D -> 2-D), host out, synchronises.  reset != 0 zeroes
+ * them afterwards.  Replaces the exchange tallies of hydrointel/solver/coupling.py:210-211. */
+int32_t his_links_exchanged(his_links* links, double* totals, int32_t reset, void* stream);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* HIS_GB300_H */

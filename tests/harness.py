@@ -89,3 +89,43 @@ def oracle_overtop(fx: dict, cfg: SolverConfig | None = None):
 def max_abs(a, b) -> float:
     a, b = np.asarray(a, dtype=np.float64), np.asarray(b, dtype=np.float64)
     return float(np.max(np.abs(a - b))) if a.size else 0.0
+
+
+def overtop_network(mod):
+    """The channel of the reference's overtopping case (benchmarks/suite.py:410-418)."""
+    xs = np.arange(20.0, 2000.0, 40.0)
+    zb = 5.0 - 0.001 * xs
+    n = len(xs)
+    r = mod.Reach("ch", xs, np.full(n, 500.0), zb - 2.0, np.full(n, 15.0), np.full(n, 1.0), np.full(n, 0.03), zb,
+                  ("inflow",), ("stage",))
+    return mod.ChannelNetwork([r], [], "ch")
+
+
+def cuda_swe2d(name: str, fx: dict | None = None, dtype=None, tile=None):
+    import torch
+    from his_gb300.infiltration import Horton
+    from his_gb300.swe2d import SWE2D
+    spec = GC.SWE2D_CASES[name]
+    fx = fx if fx is not None else load(name)
+    inp = swe2d_inputs(name, fx)
+    horton = Horton(inp["f0"], inp["fc"], inp["k"], spec["t0"]) if inp["f0"] is not None else None
+    sim = SWE2D(inp["z"], inp["n"], spec["dx"], swe2d_cfg(spec), swe2d_bcs(spec), dtype=dtype or torch.float64,
+                storage=inp["S"], horton=horton, rain_weight=inp["rain_weight"], dy=spec.get("dy"),
+                batch=spec.get("batch"), tile=tile)
+    sim.set_state(inp["h0"], inp["hu0"], inp["hv0"])
+    return sim, spec, fx
+
+
+def cuda_overtop(fx: dict, dtype=None, cfg: SolverConfig | None = None):
+    """The overtopping case on the CUDA solvers, built from the exchange fixture's bed."""
+    import torch
+    import his_gb300.channels as CH
+    from his_gb300.boundaries import all_edges
+    from his_gb300.coupling import build_links
+    from his_gb300.swe1d import SWE1D
+    from his_gb300.swe2d import SWE2D
+    p = overtop_parts(fx, cfg)
+    two = SWE2D(p.z2d, p.n2d, p.dx, p.cfg, all_edges("closed"), dtype=dtype or torch.float64)
+    one = SWE1D(overtop_network(CH), p.cfg, inflow=p.inflow, stage=p.stage)
+    links = build_links(one, two)
+    return one, two, links, p
