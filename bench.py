@@ -1,0 +1,372 @@
+"""Benchmark of the GB300-native flood-engine step.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl reference]
+
+Workload (one rank): the batched production form -- 64 storms on the seeded
+400 x 325 @ 20 m terrain, float32 state and fluxes with float64 accumulators, each
+member with its own CFL step, coupled 1-D network and weir exchange -- advanced by
+the device-resident engine (CUDA graphs).  A "step" is one engine step of every
+member.  Inputs (about 0.5 GB of state and fields touched per step) exceed the
+129 MB L2, so no flush is needed between steps.
+
+Printed (rank 0, one JSON line): cell-steps/s (whole job), storms/hour of the
+batch and of the plain float64 single-storm engine at the same resolution, the
+end-to-end rate through the drop-in C-ABI path with host buffers, the roofline of
+the dominant kernel against the measured HBM peak, SM clocks sampled during the
+timed region, and the oracle's CPU float64 rate on this host as a baseline.
+
+--impl reference times the CPU restatement of the reference's float64 step (the
+oracle, all host threads) on a bounded sample of the same workload.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+from pathlib import Path
+
+ROOT = Path(__file__).resolve().parent
+sys.path.insert(0, str(ROOT))
+
+ALG_BYTES_F32 = 64      # per member-cell-step: 11 fields read + 5 written, float32
+ALG_BYTES_F64 = 128
+LAUNCHES_PER_STEP = 5   # pre, stage 1, stage 2, 1-D substeps, post
+
+
+def parse():
+    p = argparse.ArgumentParser()
+    p.add_argument("--gpus", type=int, default=1)
+    p.add_argument("--steps", type=int, default=600)
+    p.add_argument("--warmup", type=int, default=30)
+    p.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    p.add_argument("--members", type=int, default=64)
+    p.add_argument("--storm-seconds", type=float, default=45.0, help="wall budget of the storms/hour legs")
+    p.add_argument("--cpu-seconds", type=float, default=10.0)
+    p.add_argument("--quick", action="store_true")
+    return p.parse_args()
+
+
+def dist_init():
+    import torch
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if world > 1:
+        import torch.distributed as dist
+        torch.cuda.set_device(local)
+        dist.init_process_group("nccl", device_id=torch.device("cuda", local))
+    elif torch.cuda.is_available():
+        torch.cuda.set_device(0)
+    return world, rank, local
+
+
+def barrier(world):
+    if world > 1:
+        import torch.distributed as dist
+        dist.barrier()
+
+
+def max_over_ranks(x: float, world: int) -> float:
+    if world == 1:
+        return x
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor([x], dtype=torch.float64, device="cuda")
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def peaks():
+    try:
+        d = json.loads((ROOT / "MEASURED_PEAKS.json").read_text())
+        return float(d["hbm_gbs"]), "measured"
+    except Exception:
+        return 6800.0, "fallback"
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons every 200 ms while the timed region runs."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index: int):
+        self.gpu = gpu_index
+        self.proc = None
+        self.path = None
+
+    def __enter__(self):
+        fd, self.path = tempfile.mkstemp(suffix=".csv")
+        os.close(fd)
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", f"--id={self.gpu}", f"--query-gpu={self.FIELDS}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=open(self.path, "w"), stderr=subprocess.DEVNULL)
+        except Exception:
+            self.proc = None
+        return self
+
+    def __exit__(self, *exc):
+        if self.proc is not None:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except Exception:
+                self.proc.kill()
+
+    def summary(self):
+        if not self.path or not Path(self.path).exists():
+            return None
+        rows = [r.split(",") for r in Path(self.path).read_text().strip().splitlines() if r.strip()]
+        Path(self.path).unlink(missing_ok=True)
+        sm, mx, reasons = [], [], set()
+        names = ("hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap")
+        for r in rows:
+            r = [x.strip() for x in r]
+            if len(r) < 9:
+                continue
+            try:
+                sm.append(float(r[1]))
+                mx.append(float(r[2]))
+            except ValueError:
+                continue
+            for n, v in zip(names, r[5:9]):
+                if v.lower() == "active":
+                    reasons.add(n)
+        if not sm:
+            return None
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": max(mx), "samples": len(sm),
+                "reasons": sorted(reasons)}
+
+
+def read_traffic():
+    """Per-cell DRAM traffic of the dominant kernel from the committed ncu summary."""
+    p = ROOT / "profiles" / "stage2_f32_batched_uniform.md"
+    if not p.exists():
+        return None
+    for line in p.read_text().splitlines():
+        if line.strip().startswith("traffic_bytes_per_cell:"):
+            try:
+                return float(line.split(":", 1)[1].split()[0])
+            except ValueError:
+                return None
+    return None
+
+
+def storm_rate(engine, budget_s: float):
+    """Advance until every member is done or the wall budget is spent; storms/hour from the
+    simulated-time progress (exact when the batch completes)."""
+    import torch
+    t_end = [s.t_end for s in engine.storms]
+    r0 = engine.reports()
+    t_start = [r.t for r in r0]
+    torch.cuda.synchronize()
+    w0 = time.perf_counter()
+    done = False
+    while time.perf_counter() - w0 < budget_s:
+        engine.advance(256)
+        reps = engine.reports()
+        if all(r.status != 0 for r in reps):
+            done = True
+            break
+    wall = time.perf_counter() - w0
+    reps = engine.reports()
+    frac = sum((r.t - t0) / te for r, t0, te in zip(reps, t_start, t_end))
+    return {"storms_per_hour": 3600.0 * frac / wall, "wall_s": wall, "completed": done,
+            "status": sorted({int(r.status) for r in reps}), "steps": [int(r.steps) for r in reps]}
+
+
+def cpu_oracle_rate(storm, seconds: float, threads: int):
+    """The oracle (C, OpenMP) float64 coupled step on one member, on this host's cores."""
+    sys.path.insert(0, str(ROOT / "tests"))
+    sys.path.insert(0, str(ROOT / "tests" / "golden"))
+    from oracle import oracle as O
+    import harness as H
+    O.set_threads(threads)
+    orc = H.oracle_from_storm(storm)
+    t, steps = 0.0, 0
+    orc.step(t, storm.t_end)                 # warm-up step (builds the library, pages memory in)
+    w0 = time.perf_counter()
+    while time.perf_counter() - w0 < seconds and steps < 10000:
+        t = orc.step(t, storm.t_end)
+        steps += 1
+    wall = time.perf_counter() - w0
+    return {"value": storm.cells * steps / wall, "steps": steps, "wall_s": wall}
+
+
+def e2e_dropin(storms, steps: int):
+    """Same metric through the drop-in public API (batched CoupledEngine -> C ABI, host
+    buffers): every step uploads its forcing and downloads its volumes and CFL rates."""
+    import numpy as np
+    import torch
+    from his_gb300.assembly import build_engine_batch
+    eng = build_engine_batch(storms, dtype=torch.float32)
+    B = len(storms)
+    t = 0.0
+    t_end = storms[0].t_end
+    for _ in range(2):
+        t = eng.step(t, t_end)
+    torch.cuda.synchronize()
+    w0 = time.perf_counter()
+    for _ in range(steps):
+        t = eng.step(t, t_end)
+    torch.cuda.synchronize()
+    wall = time.perf_counter() - w0
+    n_sub = eng.log.n_sub_max
+    # bytes moved per step by the drop-in calls (params in, results out)
+    h2d = B * 88 + B * 2 * 8 * n_sub        # 2-D step params, 1-D substep forcing
+    d2h = B * 8 + B * 16 + B * 40 + B * eng.links.n_links * 8 + B * 24   # rates, 1-D rates, volumes, V, 1-D volumes
+    cells = sum(s.cells for s in storms)
+    return {"value": cells * steps / wall, "unit": "cell-steps/s", "h2d_bytes_per_step": int(h2d),
+            "d2h_bytes_per_step": int(d2h), "steps": steps, "shared_dt": True}
+
+
+def run_ours(args, world, rank, local):
+    import numpy as np
+    import torch
+    from his_gb300 import workloads as W
+    from his_gb300.config import SolverConfig
+    from his_gb300.engine import FloodEngine
+    members = args.members
+    storms = W.batched_uniform(members)
+    cells = sum(s.cells for s in storms)
+    eng = FloodEngine(storms, SolverConfig(), precision="fp32", graph_steps=16)
+    eng.advance(args.warmup)
+    torch.cuda.synchronize()
+    s = torch.cuda.current_stream()
+    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    with ClockSampler(local) as clk:
+        barrier(world)
+        torch.cuda.synchronize()
+        ev0.record(s)
+        eng.advance(args.steps)
+        ev1.record(s)
+        torch.cuda.synchronize()
+        barrier(world)
+    ms = max_over_ranks(ev0.elapsed_time(ev1), world)
+    clocks = clk.summary()
+    reps = eng.reports()
+    assert all(r.status == 0 for r in reps), "a member finished or failed inside the timed region"
+    value = world * cells * args.steps / (ms / 1e3)
+    # per-kernel device times (events on the launching streams)
+    prof_steps = min(args.steps, 50)
+    kms = np.zeros(6)
+    import ctypes as C
+    from his_gb300 import _lib
+    _lib.check(eng._lib.his_engine_profile(eng._engine, prof_steps, _lib.as_p(kms), _lib.stream_handle()),
+               "his_engine_profile")
+    hbm, peak_kind = peaks()
+    stage2_s = kms[2] / prof_steps / 1e3
+    achieved = ALG_BYTES_F32 * cells / stage2_s / 1e9
+    step_s = kms[5] / prof_steps / 1e3
+    traffic = read_traffic()
+    out = {"metric": "cell-steps/s", "value": value, "unit": "cell-steps/s", "n_gpus": world, "steps": args.steps,
+           "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True, "scaling": "weak",
+           "vs_baseline": None, "dtype": "f32 (f64 accumulators, 1-D network and exchange)",
+           "data": "synthetic (seeded terrain, forcing and networks)",
+           "config": {"workload": f"batched uniform: {members} storms x 400x325 @ 20 m, coupled 1-D/2-D, "
+                                  "per-member dt", "members": members, "cells_per_step": cells,
+                      "grid": "400x325", "dx_m": 20.0, "precision": "fp32", "graph_steps": 16,
+                      "l2": "inputs larger than L2 (~0.5 GB touched per step), no flush"},
+           "gpu_launches": LAUNCHES_PER_STEP * args.steps,
+           "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s",
+                        "frac": achieved / hbm, "peak_kind": peak_kind,
+                        "traffic": traffic * cells if traffic is not None else None,
+                        "kernel": "stage_kernel<float,32,8,2> (RK stage 2 + sources + friction + CFL)",
+                        "alg_bytes_per_cell": ALG_BYTES_F32,
+                        "step_achieved": ALG_BYTES_F32 * cells / step_s / 1e9,
+                        "step_frac": ALG_BYTES_F32 * cells / step_s / 1e9 / hbm,
+                        "ms_per_step_by_kernel": {"pre": kms[0] / prof_steps, "stage1": kms[1] / prof_steps,
+                                                  "stage2": kms[2] / prof_steps, "net1d": kms[3] / prof_steps,
+                                                  "post": kms[4] / prof_steps, "step": kms[5] / prof_steps}},
+           "clocks": clocks}
+    if rank == 0 and not args.quick:
+        sr = storm_rate(eng, args.storm_seconds)
+        out["storms_per_hour"] = sr["storms_per_hour"]
+        out["storms_detail"] = {k: v for k, v in sr.items() if k != "steps"} | {
+            "mean_steps": float(np.mean(sr["steps"]))}
+        if sr["completed"]:
+            errs = [r.mass_error for r in eng.results()]
+            out["mass_error_max"] = max(errs)
+        del eng
+        torch.cuda.empty_cache()
+        plain = W.plain_full()
+        pe = FloodEngine([plain], SolverConfig(), precision="fp64", graph_steps=16)
+        pr = storm_rate(pe, args.storm_seconds)
+        out["plain_fp64_single"] = {"storms_per_hour": pr["storms_per_hour"], "completed": pr["completed"],
+                                    "wall_s": pr["wall_s"], "steps": pr["steps"][0],
+                                    "cell_steps_per_s": plain.cells * pr["steps"][0] / pr["wall_s"]}
+        out["speedup_vs_plain_fp64_single"] = out["storms_per_hour"] / pr["storms_per_hour"]
+        del pe
+        torch.cuda.empty_cache()
+        out["e2e"] = e2e_dropin(storms[: min(members, 64)], steps=20)
+        threads = os.cpu_count() or 1
+        cpu = cpu_oracle_rate(storms[0], args.cpu_seconds, threads)
+        out["cpu_baseline"] = {"value": cpu["value"], "unit": "cell-steps/s", "cores": threads, "kind": "port",
+                               "sample": f"{cpu['steps']} coupled float64 steps of one 400x325 member "
+                                         f"({cpu['wall_s']:.1f} s)"}
+    else:
+        out["e2e"] = None
+    return out
+
+
+def run_reference(args, world, rank):
+    if rank != 0:
+        return None
+    from his_gb300 import workloads as W
+    sys.path.insert(0, str(ROOT / "tests"))
+    sys.path.insert(0, str(ROOT / "tests" / "golden"))
+    from oracle import oracle as O
+    import harness as H
+    threads = os.cpu_count() or 1
+    O.set_threads(threads)
+    storm = W.batched_uniform(1)[0]
+    orc = H.oracle_from_storm(storm)
+    t = 0.0
+    for _ in range(max(1, min(args.warmup, 3))):
+        t = orc.step(t, storm.t_end)
+    steps = max(1, min(args.steps, 40))
+    w0 = time.perf_counter()
+    for _ in range(steps):
+        t = orc.step(t, storm.t_end)
+    wall = time.perf_counter() - w0
+    value = storm.cells * steps / wall
+    return {"impl": "reference", "metric": "cell-steps/s", "value": value, "unit": "cell-steps/s", "n_gpus": world,
+            "steps": steps, "warmup": args.warmup, "ms_per_step": wall * 1e3 / steps, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+            "config": {"workload": "batched uniform member: 400x325 @ 20 m, coupled 1-D/2-D (one member per step, "
+                                   "the CPU restatement of the reference's float64 step)"},
+            "cpu_baseline": {"value": value, "unit": "cell-steps/s", "cores": threads, "kind": "port",
+                             "sample": f"{steps} coupled float64 steps of one 400x325 member"},
+            "e2e": {"value": value, "unit": "cell-steps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+            "gpu_launches": 0}
+
+
+def main():
+    args = parse()
+    if args.warmup < 3:
+        args.warmup = 3
+    if args.impl == "reference":
+        world = int(os.environ.get("WORLD_SIZE", "1"))
+        rank = int(os.environ.get("RANK", "0"))
+        out = run_reference(args, world, rank)
+        if out is not None:
+            print(json.dumps(out))
+        return
+    world, rank, local = dist_init()
+    out = run_ours(args, world, rank, local)
+    if rank == 0:
+        print(json.dumps(out))
+    if world > 1:
+        import torch.distributed as dist
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

@@ -37,7 +37,7 @@ class GridDesc(C.Structure):
     _fields_ = [("ny", C.c_int32), ("nx", C.c_int32), ("bc", C.c_int32 * 4), ("dx", C.c_double),
                 ("dy", C.c_double), ("horton_t0", C.c_double)] + \
                [(n, C.c_void_p) for n in ("h", "hu", "hv", "s_filled", "infil_cum", "z", "manning", "storage",
-                                         "f0", "fc", "k", "rain_weight")]
+                                         "f0", "fc", "k", "rain_weight", "peak_h", "peak_speed")]
 
 
 class StepParams(C.Structure):
@@ -56,6 +56,23 @@ class LinksDesc(C.Structure):
     _fields_ = [("n_links", C.c_int32), ("n_unique", C.c_int32), ("cell1d", _I32P), ("inv", _I32P),
                 ("uniq", _I64P), ("zbank", _F64P), ("length", _F64P), ("z2", _F64P)]
 
+
+class ForcingDesc(C.Structure):
+    _fields_ = [("t0", C.c_double), ("t_end", C.c_double), ("rain_t0", C.c_double), ("rain_step", C.c_double),
+                ("rain_n", C.c_int32), ("tide_on", C.c_int32), ("rain", _F64P), ("tide_n", C.c_int32),
+                ("q_n", C.c_int32), ("tide_base", C.c_double), ("tide_shift", C.c_double),
+                ("tide_amp", C.c_double * 4), ("tide_w", C.c_double * 4), ("tide_phase", C.c_double * 4),
+                ("q_t0", C.c_double), ("q_step", C.c_double), ("q", _F64P), ("edge_src", C.c_int32 * 4),
+                ("edge_val", C.c_double * 4)]
+
+
+class MemberReport(C.Structure):
+    _fields_ = [("t", C.c_double), ("dt_last", C.c_double), ("dt_min", C.c_double), ("dt_max", C.c_double),
+                ("rate", C.c_double), ("steps", C.c_int64), ("status", C.c_int32), ("n_sub_max", C.c_int32),
+                ("n_dt_clamped", C.c_int32), ("pad", C.c_int32), ("acc", C.c_double * 7)]
+
+
+STATUS = {0: "running", 1: "done", 2: "non-finite state", 3: "implausible state", 4: "too many 1-D substeps"}
 
 # entry point -> (restype, argtypes); the exact set declared in include/his_gb300.h
 _H = C.c_void_p
@@ -78,6 +95,12 @@ SIGNATURES = {
     "his_links_destroy": (C.c_int32, [_H]),
     "his_exchange": (C.c_int32, [_H, C.POINTER(SolverCfg), C.c_double, _F64P, C.c_void_p]),
     "his_links_exchanged": (C.c_int32, [_H, _F64P, C.c_int32, C.c_void_p]),
+    "his_engine_create": (C.c_int32, [_H, _H, _H, C.c_int32, C.POINTER(ForcingDesc), C.c_int32, C.c_int32,
+                                      C.POINTER(_H)]),
+    "his_engine_destroy": (C.c_int32, [_H]),
+    "his_engine_advance": (C.c_int32, [_H, C.c_int32, C.c_void_p]),
+    "his_engine_report": (C.c_int32, [_H, C.POINTER(MemberReport), C.c_void_p]),
+    "his_engine_profile": (C.c_int32, [_H, C.c_int32, _F64P, C.c_void_p]),
 }
 
 _LIB = None

@@ -26,7 +26,7 @@ COMMON = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-Xptxas", "-
 UNITS = {
     "capi.cu": [],
     "swe2d_f64.cu": ["-fmad=false"],
-    "swe2d_f32.cu": ["-fmad=true"],
+    "swe2d_f32.cu": ["-fmad=true", "--use_fast_math"],
     "net1d.cu": ["-fmad=false"],
 }
 

@@ -156,6 +156,7 @@ static int upload_params(his_grid* g, const his_step_params* p, cudaStream_t s) 
         sp[m].dt = q.dt; sp[m].t = q.t; sp[m].rain = q.rain;
         for (int e = 0; e < 4; ++e) { sp[m].bc0[e] = q.bc_t[e]; sp[m].bc1[e] = q.bc_t_dt[e]; }
         sp[m].active = 1;
+        params_set_f32(sp[m]);
     }
     // pageable source: returns once the data is staged, so `sp` may go out of scope
     HIS_CK(cudaMemcpyAsync(g->d_params, sp.data(), sizeof(StepParams) * g->n, cudaMemcpyHostToDevice, s));
@@ -457,6 +458,169 @@ int32_t his_links_exchanged(his_links* L, double* totals, int32_t reset, void* s
     HIS_CK(cudaStreamSynchronize(s));
     std::memcpy(totals, L->h_V, sizeof(double) * 2 * L->n);
     if (reset) HIS_CK(cudaMemsetAsync(L->d_exch, 0, sizeof(double) * 2 * L->n, s));
+    return HIS_OK;
+}
+
+}  // extern "C"
+
+// ------------------------------------------------------------------------ engine
+extern "C" {
+
+int32_t his_engine_destroy(his_engine* E) {
+    if (!E) return HIS_OK;
+    if (E->s0) cudaStreamSynchronize(E->s0);
+    if (E->s1) cudaStreamSynchronize(E->s1);
+    if (E->exec) cudaGraphExecDestroy(E->exec);
+    cudaFree(E->d_em);
+    cudaFree(E->d_arena);
+    cudaFree(E->d_netf);
+    cudaFree(E->d_vol1d);
+    if (E->h_em) cudaFreeHost(E->h_em);
+    for (cudaEvent_t ev : {E->ev_fork, E->ev_join, E->ev_in, E->ev_out})
+        if (ev) cudaEventDestroy(ev);
+    if (E->s0) cudaStreamDestroy(E->s0);
+    if (E->s1) cudaStreamDestroy(E->s1);
+    delete E;
+    return HIS_OK;
+}
+
+int32_t his_engine_create(his_grid* grid, his_net* net, his_links* links, int32_t n_members,
+                          const his_forcing_desc* forcing, int32_t max_sub, int32_t graph_steps, his_engine** out) {
+    if (!out) return bad("out is NULL");
+    *out = nullptr;
+    if (!grid || !forcing) return bad("grid and forcing are required");
+    if (n_members != grid->n) return bad("forcing must be given for every grid member");
+    if (net && net->n != n_members) return bad("network set and grid set differ in members");
+    if (links && (!net || links->grid != grid || links->net != net)) return bad("links must bind this grid and network");
+    if (max_sub == 0) max_sub = 64;
+    if (max_sub < 1 || max_sub > 4096) return bad("max_sub must be in [1, 4096]");
+    if (graph_steps == 0) graph_steps = 16;
+    if (graph_steps < 1 || graph_steps > 1024) return bad("graph_steps must be in [1, 1024]");
+    Arena ar;
+    std::vector<size_t> orain(n_members), oq(n_members);
+    std::vector<EngMember> H(n_members);
+    for (int m = 0; m < n_members; ++m) {
+        const his_forcing_desc& f = forcing[m];
+        std::string who = "member " + std::to_string(m) + ": ";
+        if (!std::isfinite(f.t0) || !std::isfinite(f.t_end) || !(f.t_end >= f.t0)) return bad(who + "need t0 <= t_end");
+        if (f.rain_n < 0 || (f.rain_n > 0 && (!f.rain || !(f.rain_step > 0)))) return bad(who + "bad rain table");
+        if (f.q_n < 0 || (f.q_n > 0 && (!f.q || !(f.q_step > 0)))) return bad(who + "bad inflow table");
+        if (f.tide_n < 0 || f.tide_n > 4) return bad(who + "at most 4 tidal constituents");
+        for (int e = 0; e < 4; ++e)
+            if (f.edge_src[e] < 0 || f.edge_src[e] > 2) return bad(who + "edge value source must be 0, 1 or 2");
+        orain[m] = ar.add(f.rain, sizeof(double) * std::max(f.rain_n, 0));
+        oq[m] = ar.add(f.q, sizeof(double) * std::max(f.q_n, 0));
+        EngMember& E = H[m];
+        std::memset(&E, 0, sizeof(E));
+        E.rain_t0 = f.rain_t0; E.rain_step = f.rain_step; E.rain_n = f.rain_n;
+        E.tide_on = f.tide_on; E.tide_n = f.tide_n; E.tide_base = f.tide_base; E.tide_shift = f.tide_shift;
+        for (int j = 0; j < 4; ++j) { E.amp[j] = f.tide_amp[j]; E.w[j] = f.tide_w[j]; E.ph[j] = f.tide_phase[j]; }
+        E.q_t0 = f.q_t0; E.q_step = f.q_step; E.q_n = f.q_n;
+        for (int e = 0; e < 4; ++e) { E.edge_src[e] = f.edge_src[e]; E.edge_val[e] = f.edge_val[e]; }
+        E.t_end = f.t_end;
+        E.t = f.t0;
+        E.dt_min = INFINITY;
+        E.status = f.t_end - f.t0 > 1e-9 ? ST_RUNNING : ST_DONE;
+    }
+    his_engine* E = new his_engine();
+    E->grid = grid; E->net = net; E->links = links; E->n = n_members; E->max_sub = max_sub;
+    E->graph_steps = graph_steps;
+    E->pre_smem = std::max<size_t>(links ? links->smem : 0, sizeof(double) * 64);
+    auto fail = [&](cudaError_t e, const char* w) { int r = cuda_fail(e, w); his_engine_destroy(E); return r; };
+    cudaError_t e = cudaMalloc(&E->d_arena, std::max<size_t>(ar.host.size(), 256));
+    if (e == cudaSuccess && ar.host.size())
+        e = cudaMemcpy(E->d_arena, ar.host.data(), ar.host.size(), cudaMemcpyHostToDevice);
+    if (e != cudaSuccess) return fail(e, "his_engine_create: forcing tables");
+    for (int m = 0; m < n_members; ++m) {
+        H[m].rain = forcing[m].rain_n > 0 ? (const double*)((char*)E->d_arena + orain[m]) : nullptr;
+        H[m].q = forcing[m].q_n > 0 ? (const double*)((char*)E->d_arena + oq[m]) : nullptr;
+    }
+    e = cudaMalloc(&E->d_em, sizeof(EngMember) * n_members);
+    if (e == cudaSuccess) e = cudaMemcpy(E->d_em, H.data(), sizeof(EngMember) * n_members, cudaMemcpyHostToDevice);
+    if (e == cudaSuccess) e = cudaMallocHost(&E->h_em, sizeof(EngMember) * n_members);
+    if (e == cudaSuccess) e = cudaMalloc(&E->d_netf, sizeof(double) * 2 * (size_t)max_sub * n_members);
+    if (e == cudaSuccess) e = cudaMalloc(&E->d_vol1d, sizeof(double) * 3 * n_members);
+    if (e == cudaSuccess) e = cudaMemset(E->d_vol1d, 0, sizeof(double) * 3 * n_members);
+    if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&E->s0, cudaStreamNonBlocking);
+    if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&E->s1, cudaStreamNonBlocking);
+    for (cudaEvent_t* ev : {&E->ev_fork, &E->ev_join, &E->ev_in, &E->ev_out})
+        if (e == cudaSuccess) e = cudaEventCreateWithFlags(ev, cudaEventDisableTiming);
+    if (e != cudaSuccess) return fail(e, "his_engine_create: allocation");
+    int rc = net_engine_prepare(E);
+    if (rc == HIS_OK) rc = grid->prec == HIS_PREC_F64 ? engine_take_rate_f64(E) : engine_take_rate_f32(E);
+    if (rc == HIS_OK) {
+        e = cudaStreamSynchronize(E->s0);
+        if (e != cudaSuccess) rc = cuda_fail(e, "his_engine_create: initial rate");
+    }
+    if (rc != HIS_OK) {
+        his_engine_destroy(E);
+        return rc;
+    }
+    *out = E;
+    return HIS_OK;
+}
+
+static int engine_enqueue(his_engine* E, int n) {
+    return E->grid->prec == HIS_PREC_F64 ? engine_enqueue_f64(E, n) : engine_enqueue_f32(E, n);
+}
+
+int32_t his_engine_advance(his_engine* E, int32_t n_steps, void* stream) {
+    if (!E) return bad("engine is NULL");
+    if (n_steps < 0) return bad("n_steps must be >= 0");
+    cudaStream_t caller = (cudaStream_t)stream;
+    HIS_CK(cudaEventRecord(E->ev_in, caller));
+    HIS_CK(cudaStreamWaitEvent(E->s0, E->ev_in, 0));
+    if (!E->exec && n_steps >= E->graph_steps) {
+        cudaGraph_t graph = nullptr;
+        HIS_CK(cudaStreamBeginCapture(E->s0, cudaStreamCaptureModeThreadLocal));
+        int rc = engine_enqueue(E, E->graph_steps);
+        cudaError_t ce = cudaStreamEndCapture(E->s0, &graph);
+        if (rc) { if (graph) cudaGraphDestroy(graph); return rc; }
+        if (ce != cudaSuccess) return cuda_fail(ce, "his_engine_advance: capture");
+        ce = cudaGraphInstantiate(&E->exec, graph, 0);
+        cudaGraphDestroy(graph);
+        if (ce != cudaSuccess) { E->exec = nullptr; return cuda_fail(ce, "his_engine_advance: instantiate"); }
+    }
+    int done = 0;
+    if (E->exec) {
+        for (; done + E->graph_steps <= n_steps; done += E->graph_steps) HIS_CK(cudaGraphLaunch(E->exec, E->s0));
+    }
+    if (done < n_steps) {
+        int rc = engine_enqueue(E, n_steps - done);
+        if (rc) return rc;
+    }
+    HIS_CK(cudaEventRecord(E->ev_out, E->s0));
+    HIS_CK(cudaStreamWaitEvent(caller, E->ev_out, 0));
+    return HIS_OK;
+}
+
+int32_t his_engine_report(his_engine* E, his_member_report* reports, void* stream) {
+    if (!E || !reports) return bad("engine and reports are required");
+    cudaStream_t caller = (cudaStream_t)stream;
+    HIS_CK(cudaEventRecord(E->ev_in, caller));
+    HIS_CK(cudaStreamWaitEvent(E->s0, E->ev_in, 0));
+    HIS_CK(cudaMemcpyAsync(E->h_em, E->d_em, sizeof(EngMember) * E->n, cudaMemcpyDeviceToHost, E->s0));
+    HIS_CK(cudaStreamSynchronize(E->s0));
+    for (int m = 0; m < E->n; ++m) {
+        const EngMember& M = E->h_em[m];
+        his_member_report& r = reports[m];
+        r.t = M.t; r.dt_last = M.dt; r.dt_min = M.dt_min; r.dt_max = M.dt_max; r.rate = M.rate;
+        r.steps = M.steps; r.status = M.status; r.n_sub_max = M.n_sub_max; r.n_dt_clamped = M.n_clamped; r.pad = 0;
+        for (int j = 0; j < 7; ++j) r.acc[j] = M.acc[j];
+    }
+    return HIS_OK;
+}
+
+int32_t his_engine_profile(his_engine* E, int32_t n_steps, double* ms, void* stream) {
+    if (!E || !ms) return bad("engine and ms are required");
+    if (n_steps < 0) return bad("n_steps must be >= 0");
+    cudaStream_t caller = (cudaStream_t)stream;
+    HIS_CK(cudaEventRecord(E->ev_in, caller));
+    HIS_CK(cudaStreamWaitEvent(E->s0, E->ev_in, 0));
+    for (int j = 0; j < 6; ++j) ms[j] = 0.0;
+    int rc = E->grid->prec == HIS_PREC_F64 ? engine_profile_f64(E, n_steps, ms) : engine_profile_f32(E, n_steps, ms);
+    if (rc) return rc;
+    HIS_CK(cudaStreamSynchronize(E->s0));
     return HIS_OK;
 }
 

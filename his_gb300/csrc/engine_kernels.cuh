@@ -1,0 +1,152 @@
+// Device-resident coupled time loop: every member advances with its own dt, chosen,
+// forced and accounted for on the GPU, so K steps run as one CUDA graph with no
+// host round trip.  One step is
+//
+//   eng_pre   (one CTA per member)  2-D CFL dt from the rate of the current state,
+//             1-D CFL and substep count, weir exchange, forcing at t, t+dt and at the
+//             1-D substep starts                          (coupling.py:201-212)
+//   stage 1, stage 2 (tiles of every member)              (swe2d.py:305-371)
+//   net substeps (one CTA per member, concurrent with the 2-D stages)
+//                                                         (coupling.py:216-221)
+//   eng_post  (one warp per member)  step volumes summed in tile order into the
+//             float64 accumulators, t += dt, plausibility (coupling.py:213-227, :169-192)
+#pragma once
+#include "net1d_kernels.cuh"
+#include "swe2d_kernels.cuh"
+
+namespace his {
+
+__host__ __device__ inline size_t eng_pre_smem_bytes(size_t exchange_bytes) {
+    size_t r = sizeof(double) * 64;
+    return exchange_bytes > r ? exchange_bytes : r;
+}
+
+template <class R>
+__global__ void eng_pre_kernel(EngMember* __restrict__ em, StepParams* __restrict__ params,
+                               const Grid<R>* __restrict__ grids, const Net* __restrict__ nets,
+                               const Lnk* __restrict__ links, Consts c, double* __restrict__ netf, int max_sub,
+                               double* __restrict__ exch) {
+    extern __shared__ double sm[];
+    __shared__ int s_go, s_nsub;
+    __shared__ double s_dt;
+    const int m = blockIdx.x;
+    EngMember& E = em[m];
+    if (threadIdx.x == 0) {
+        s_go = E.status == ST_RUNNING;
+        if (!s_go) params[m].active = 0;
+        double rate = E.rate;
+        double dt = rate > 0.0 ? c.cfl / rate : c.dt_max;
+        if (dt < c.dt_min || dt > c.dt_max) {
+            if (dt < c.dt_min && s_go) E.n_clamped++;
+            dt = fmin(fmax(dt, c.dt_min), c.dt_max);
+        }
+        s_dt = fmin(dt, E.t_end - E.t);
+        s_nsub = 0;
+    }
+    __syncthreads();
+    if (!s_go) return;
+    const double dt = s_dt;
+    if (nets) {
+        double r1 = 0.0;
+        bool wet = false;
+        net_rate_dev(nets[m], c, r1, wet, sm);
+        if (threadIdx.x == 0) {
+            const double dt1 = wet ? fmin(c.cfl_1d / r1, c.dt_max) : c.dt_max;
+            const double ns = ceil(dt / dt1 - 1e-9);
+            s_nsub = ns < 1.0 ? 1 : (ns > (double)max_sub ? max_sub + 1 : (int)ns);
+        }
+        __syncthreads();
+        if (s_nsub > max_sub) {
+            if (threadIdx.x == 0) {
+                E.status = ST_SUBSTEPS;
+                params[m].active = 0;
+            }
+            return;
+        }
+        if (links) exchange_dev<R>(links[m], nets[m], grids[m], c, dt, nullptr, exch, m, sm);
+        const double sub = dt / s_nsub;
+        for (int k = threadIdx.x; k < s_nsub; k += blockDim.x) {
+            const double tk = E.t + k * sub;
+            netf[((size_t)m * max_sub + k) * 2 + 0] = eng_inflow(E, tk);
+            netf[((size_t)m * max_sub + k) * 2 + 1] = eng_tide(E, tk);
+        }
+    }
+    if (threadIdx.x == 0) {
+        StepParams& P = params[m];
+        P.dt = dt;
+        P.t = E.t;
+        P.rain = eng_rain(E, E.t);
+        for (int e = 0; e < 4; ++e) {
+            P.bc0[e] = eng_edge(E, e, E.t);
+            P.bc1[e] = eng_edge(E, e, E.t + dt);
+        }
+        P.active = 1;
+        params_set_f32(P);
+        E.dt = dt;
+        E.n_sub = s_nsub;
+    }
+}
+
+template <class R>
+__global__ void eng_post_kernel(EngMember* __restrict__ em, const StepParams* __restrict__ params,
+                                const Grid<R>* __restrict__ grids, Consts c, const double* __restrict__ partials,
+                                const double* __restrict__ vol1d, double* __restrict__ out) {
+    const int m = blockIdx.x, lane = threadIdx.x;
+    if (!params[m].active) return;
+    const Grid<R>& gd = grids[m];
+    double s[NPART];
+#pragma unroll
+    for (int j = 0; j < NPART; ++j) s[j] = 0.0;
+    for (int t = lane; t < gd.n_tiles; t += 32) {
+        const double* p = partials + (size_t)(gd.tile0 + t) * NPART;
+#pragma unroll
+        for (int j = 0; j < NPART; ++j) s[j] = (j == P_RATE || j == P_HMAX) ? fmax(s[j], p[j]) : s[j] + p[j];
+    }
+#pragma unroll
+    for (int j = 0; j < NPART; ++j) s[j] = (j == P_RATE || j == P_HMAX) ? warp_max(s[j]) : warp_sum(s[j]);
+    if (lane != 0) return;
+    EngMember& E = em[m];
+    const StepParams& pr = params[m];
+    const double dt = (double)R(pr.dt);
+    double qin = s[P_XIN1] * gd.dy + s[P_YIN1] * gd.dx;
+    double qout = s[P_XOUT1] * gd.dy + s[P_YOUT1] * gd.dx;
+    double clip = s[P_CLIP1] * gd.area;
+    if (c.order == 2) {
+        qin = 0.5 * (qin + (s[P_XIN2] * gd.dy + s[P_YIN2] * gd.dx));
+        qout = 0.5 * (qout + (s[P_XOUT2] * gd.dy + s[P_YOUT2] * gd.dx));
+        clip = clip + s[P_CLIP2] * gd.area;
+    }
+    const double rain = gd.rw ? s[P_RAINW] * gd.area
+                              : (double)(R(pr.rain) * R(pr.dt)) * ((double)((long long)gd.nx * gd.ny) * gd.area);
+    const double infil = s[P_INFIL] * gd.area;
+    E.acc[0] += rain;
+    E.acc[1] += infil;
+    E.acc[2] += qin * dt;
+    E.acc[3] += qout * dt;
+    E.acc[6] += clip;
+    if (vol1d && E.n_sub > 0) {
+        E.acc[4] += vol1d[m * 3 + 0];
+        E.acc[5] += vol1d[m * 3 + 1];
+        E.acc[6] += vol1d[m * 3 + 2];
+    }
+    E.rate = s[P_RATE];
+    E.t = E.t + E.dt;
+    E.steps += 1;
+    E.dt_min = fmin(E.dt_min, E.dt);
+    E.dt_max = fmax(E.dt_max, E.dt);
+    E.n_sub_max = max(E.n_sub_max, E.n_sub);
+    double* o = out + (size_t)m * 8;
+    o[0] = qin * dt; o[1] = qout * dt; o[2] = rain; o[3] = infil; o[4] = clip;
+    o[5] = s[P_RATE]; o[6] = s[P_HSUM] * gd.area; o[7] = s[P_SSUM] * gd.area;
+    if (!isfinite(s[P_HSUM]) || !isfinite(s[P_RATE])) E.status = ST_NONFINITE;
+    else if (s[P_HMAX] > MAX_PLAUSIBLE_DEPTH_2D) E.status = ST_IMPLAUSIBLE;
+    else if (E.t >= E.t_end - 1e-9) E.status = ST_DONE;
+}
+
+// Copy the rate of the current state (finalize output, mode 1) into the engine records.
+static __global__ void eng_take_rate_kernel(EngMember* __restrict__ em, const double* __restrict__ out, int n) {
+    const int m = blockIdx.x * blockDim.x + threadIdx.x;
+    if (m < n) em[m].rate = out[(size_t)m * 8 + 5];
+}
+
+}  // namespace his

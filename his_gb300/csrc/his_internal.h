@@ -53,6 +53,22 @@ struct his_links {
     size_t smem = 0;
 };
 
+struct his_engine {
+    his_grid* grid = nullptr;
+    his_net* net = nullptr;
+    his_links* links = nullptr;
+    int n = 0, max_sub = 64, graph_steps = 16;
+    his::EngMember* d_em = nullptr;
+    his::EngMember* h_em = nullptr;          // pinned
+    void* d_arena = nullptr;
+    double* d_netf = nullptr;                // n x max_sub x 2 substep forcing
+    double* d_vol1d = nullptr;               // n x 3
+    size_t pre_smem = 0;
+    cudaStream_t s0 = nullptr, s1 = nullptr;
+    cudaEvent_t ev_fork = nullptr, ev_join = nullptr, ev_in = nullptr, ev_out = nullptr;
+    cudaGraphExec_t exec = nullptr;
+};
+
 namespace his {
 
 void set_error(const std::string& msg);
@@ -81,8 +97,17 @@ int exchange_f64(his_links* l, const Consts& c, double dt, cudaStream_t s);
 int exchange_f32(his_links* l, const Consts& c, double dt, cudaStream_t s);
 size_t stage_smem_bytes(int prec, int tx, int ty);
 
+int engine_enqueue_f64(his_engine* e, int n_steps);
+int engine_enqueue_f32(his_engine* e, int n_steps);
+int engine_take_rate_f64(his_engine* e);
+int engine_take_rate_f32(his_engine* e);
+int engine_profile_f64(his_engine* e, int n_steps, double* ms);
+int engine_profile_f32(his_engine* e, int n_steps, double* ms);
+
 // net1d.cu
 int net_step_launch(his_net* n, double dt, int n_sub, cudaStream_t s);
 int net_reduce_launch(his_net* n, cudaStream_t s);
+int net_engine_launch(his_engine* e, cudaStream_t s);
+int net_engine_prepare(his_engine* e);
 
 }  // namespace his

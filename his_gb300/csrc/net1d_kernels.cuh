@@ -119,6 +119,134 @@ __host__ __device__ inline size_t net_smem_bytes(int n_cells, int n_faces) {
     return sizeof(double) * (7 * (size_t)n_cells + 4 * (size_t)n_faces + 32 * 4);
 }
 
+// n_sub substeps of dt/n_sub each for the network N, run by the whole CTA.
+// forcing: per substep (inflow, stage).  vols (thread 0, if non-NULL): bnd_in,
+// bnd_out, clip summed over the substeps.  sm: net_smem_bytes() of shared memory.
+__device__ __forceinline__ void net_substeps_dev(const Net& N, const Consts& c, double dt_total, int n_sub,
+                                                 const double* __restrict__ forcing, double* vols, double* sm) {
+    const int nc = N.n_cells, nf = N.n_faces, tid = threadIdx.x, nt = blockDim.x;
+    double *A = sm, *Q = A + nc, *Ag = Q + nc, *Qg = Ag + nc, *yv = Qg + nc, *uv = yv + nc, *th = uv + nc;
+    double *F1 = th + nc, *F2 = F1 + nf, *pL = F2 + nf, *pR = pL + nf, *red = pR + nf;
+    const Sec s{N.b, N.m, N.yb, N.ts}, fs{N.fb, N.fm, N.fyb, N.fts};
+    const double g = c.g, dt = dt_total / n_sub;
+    for (int i = tid; i < nc; i += nt) { A[i] = N.A[i]; Q[i] = N.Q[i]; }
+    __syncthreads();
+    double tot_in = 0.0, tot_out = 0.0, tot_clip = 0.0;
+    for (int k = 0; k < n_sub; ++k) {
+        const double q_in = forcing[2 * k + 0];
+        const double eta = forcing[2 * k + 1];
+        // ghost cells from the interior neighbour (swe1d.py:265-294)
+        for (int i = tid; i < nc; i += nt) {
+            const int kd = N.kind[i];
+            if (kd < 2) { Ag[i] = A[i]; Qg[i] = Q[i]; continue; }
+            const int src = N.gsrc[i];
+            const double As = A[src], Qs = Q[src], sg = N.gsign[i];
+            const double ys = sec_depth(s, i, As);
+            const double un = sg * vel1d(c, s, i, As, Qs);
+            const bool wet_i = ys >= c.h_dry;
+            double An, Qn;
+            if (kd == 3) {
+                double yst = clamp0(eta - N.z[i]);
+                double Ast = sec_area(s, i, yst);
+                double ci = sqrt(g * As / sec_top(s, i, ys));
+                double cg = sqrt(g * Ast / sec_top(s, i, yst));
+                double un_st = wet_i ? un + 2.0 * (ci - cg) : 0.0;
+                if (wet_i && (un > ci)) { un_st = un; Ast = As; }
+                if (!(sec_depth(s, i, Ast) >= c.h_dry)) un_st = 0.0;
+                An = Ast;
+                Qn = sg * Ast * un_st;
+            } else if (kd == 2) {
+                double yc = fmax(pow(q_in * q_in / (g * N.b[i] * N.b[i]), 1.0 / 3.0), c.h_dry);
+                An = wet_i ? As : sec_area(s, i, yc);
+                Qn = -sg * q_in;
+            } else {
+                An = As;
+                Qn = -Qs;
+            }
+            Ag[i] = An;
+            Qg[i] = Qn;
+        }
+        __syncthreads();
+        for (int i = tid; i < nc; i += nt) {
+            yv[i] = sec_depth(s, i, Ag[i]);
+            uv[i] = vel1d(c, s, i, Ag[i], Qg[i]);
+        }
+        __syncthreads();
+        // face fluxes with hydrostatic reconstruction (swe1d.py:326-336)
+        for (int f = tid; f < nf; f += nt) {
+            const int l = N.fl[f], r = N.fr[f];
+            const double zL = N.z[l], zR = N.z[r], zf = rmax(zL, zR);
+            const double yL = clamp0(zL + yv[l] - zf), yR = clamp0(zR + yv[r] - zf);
+            const double AL = sec_area(fs, f, yL), AR = sec_area(fs, f, yR);
+            const double uL = uv[l], uR = uv[r];
+            pL[f] = g * sec_i1(fs, f, yL);
+            pR[f] = g * sec_i1(fs, f, yR);
+            const double cL = sqrt(g * AL / sec_top(fs, f, yL));
+            const double cR = sqrt(g * AR / sec_top(fs, f, yR));
+            hll_1d(AL, AL * uL, pL[f], cL, AR, AR * uR, pR[f], cR, uL, uR, F1[f], F2[f]);
+        }
+        __syncthreads();
+        // outflow limiter; ghosts unlimited (swe1d.py:337-344)
+        for (int i = tid; i < nc; i += nt) {
+            double out = 0.0;
+            for (int j = N.lstart[i]; j < N.lstart[i + 1]; ++j) out += relu(F1[N.lidx[j]]);
+            for (int j = N.rstart[i]; j < N.rstart[i + 1]; ++j) out += relu(-F1[N.ridx[j]]);
+            const double vol = Ag[i] * N.dx[i];
+            const double need = out * dt;
+            const double t = need > vol ? vol / (need > 0.0 ? need : 1.0) : 1.0;
+            th[i] = N.kind[i] >= 2 ? 1.0 : t;
+        }
+        __syncthreads();
+        double bsum[3] = {0.0, 0.0, 0.0};
+        for (int f = tid; f < nf; f += nt) {
+            const double sc = F1[f] > 0.0 ? th[N.fl[f]] : th[N.fr[f]];
+            const double Fs = F1[f] * sc;
+            F1[f] = Fs;
+            if (N.kind[N.fl[f]] >= 2) { bsum[0] += relu(Fs); bsum[1] += relu(-Fs); }
+            if (N.kind[N.fr[f]] >= 2) { bsum[0] += relu(-Fs); bsum[1] += relu(Fs); }
+        }
+        __syncthreads();
+        // update, clip, semi-implicit friction; ghosts keep their filled state (swe1d.py:345-368)
+        for (int i = tid; i < nc; i += nt) {
+            double dA = 0.0, dQ = 0.0;
+            for (int j = N.lstart[i]; j < N.lstart[i + 1]; ++j) dA += -F1[N.lidx[j]];
+            for (int j = N.rstart[i]; j < N.rstart[i + 1]; ++j) dA += F1[N.ridx[j]];
+            for (int j = N.lstart[i]; j < N.lstart[i + 1]; ++j) { int f = N.lidx[j]; dQ += -(F2[f] - pL[f]); }
+            for (int j = N.rstart[i]; j < N.rstart[i + 1]; ++j) { int f = N.ridx[j]; dQ += F2[f] - pR[f]; }
+            const int kd = N.kind[i];
+            double A1 = Ag[i] + dt * dA / N.dx[i];
+            double Q1 = Qg[i] + dt * dQ / N.dx[i];
+            const double neg = clamp0(-A1);
+            bsum[2] += neg * N.dx[i] * (kd >= 2 ? 0.0 : 1.0);
+            A1 = A1 + neg;
+            const double y1 = sec_depth(s, i, A1);
+            const double Ac = fmax(A1, 1e-12);
+            const double R = Ac / sec_perim(s, i, y1);
+            const double nm = N.nman[i];
+            const double denom = 1.0 + dt * g * (nm * nm) * fabs(Q1) / (Ac * pow(fmax(R, c.h_dry), 4.0 / 3.0));
+            Q1 = Q1 / denom;
+            if (!((y1 >= c.h_dry) && kd != 1)) Q1 = 0.0;
+            if (kd >= 2) { A1 = Ag[i]; Q1 = Qg[i]; }
+            A[i] = A1;
+            Q[i] = Q1;
+        }
+        block_sum<3>(bsum, red);
+        if (tid == 0) {
+            tot_in += bsum[0] * dt;
+            tot_out += bsum[1] * dt;
+            tot_clip += bsum[2];
+        }
+    }
+    __syncthreads();
+    for (int i = tid; i < nc; i += nt) { N.A[i] = A[i]; N.Q[i] = Q[i]; }
+    if (tid == 0 && vols) {
+        vols[0] = tot_in;
+        vols[1] = tot_out;
+        vols[2] = tot_clip;
+    }
+}
+
+
 __host__ __device__ inline size_t exchange_smem_bytes(int n_links, int n_unique, int n_cells) {
     return sizeof(double) * (2 * (size_t)n_links + 2 * (size_t)n_unique + (size_t)n_cells + 32 * 2);
 }
@@ -127,16 +255,8 @@ __host__ __device__ inline size_t exchange_smem_bytes(int n_links, int n_unique,
 // (params) when params is non-NULL, else dt_host.  V: per-link volumes at
 // lnk.v_offset; exch: per member (2-D -> 1-D total, 1-D -> 2-D total).
 template <class R>
-__global__ void exchange_kernel(const Lnk* __restrict__ links, const Net* __restrict__ nets,
-                                const Grid<R>* __restrict__ grids, const StepParams* __restrict__ params, Consts c,
-                                double dt_host, double* __restrict__ Vout, double* __restrict__ exch) {
-    extern __shared__ double sm[];
-    const int mb = blockIdx.x;
-    const Lnk& L = links[mb];
-    const Net& N = nets[mb];
-    const Grid<R>& gd = grids[mb];
-    if (params && !params[mb].active) return;
-    const double dt = params ? params[mb].dt : dt_host;
+__device__ __forceinline__ void exchange_dev(const Lnk& L, const Net& N, const Grid<R>& gd, const Consts& c, double dt,
+                                             double* __restrict__ Vout, double* __restrict__ exch, int mb, double* sm) {
     const int nl = L.n_links, nu = L.n_unique, nc = N.n_cells, tid = threadIdx.x, nt = blockDim.x;
     double *V = sm, *sg = V + nl, *hu_ = sg + nl, *f2 = hu_ + nu, *f1 = f2 + nu, *red = f1 + nc;
     const Sec s{N.b, N.m, N.yb, N.ts};
@@ -153,7 +273,15 @@ __global__ void exchange_kernel(const Lnk* __restrict__ links, const Net* __rest
         const double up = rmax(eta1, eta2), dn = rmin(eta1, eta2);
         const double d_up = clamp0(up - zb), d_dn = clamp0(dn - zb);
         const double ratio = d_up > 0.0 ? d_dn / d_up : 0.0;
-        const double q = c.weir_cw * L.length[l] * pow(d_up, 1.5) * pow(clamp0(1.0 - pow(ratio, 1.5)), 0.385);
+        double q;
+        if constexpr (sizeof(R) == 8) {
+            q = c.weir_cw * L.length[l] * pow(d_up, 1.5) * pow(clamp0(1.0 - pow(ratio, 1.5)), 0.385);
+        } else {
+            // production form: the weir law's powers in float32 (the FP64 pipe is ~1/64 rate)
+            const float df = (float)d_up, rf = (float)ratio;
+            const float sub = powf(fmaxf(1.0f - rf * sqrtf(rf), 0.0f), 0.385f);
+            q = (double)((float)(c.weir_cw * L.length[l]) * (df * sqrtf(df)) * sub);
+        }
         sg[l] = eta2 > eta1 ? 1.0 : -1.0;
         double v = q * dt;
         const double plan1 = (y1 <= N.yb[c1] ? N.b[c1] + 2.0 * N.m[c1] * y1 : N.ts[c1]) * N.dx[c1];
@@ -207,6 +335,45 @@ __global__ void exchange_kernel(const Lnk* __restrict__ links, const Net* __rest
         exch[mb * 2 + 0] += ex[0];
         exch[mb * 2 + 1] += ex[1];
     }
+    __syncthreads();
+}
+
+template <class R>
+__global__ void exchange_kernel(const Lnk* __restrict__ links, const Net* __restrict__ nets,
+                                const Grid<R>* __restrict__ grids, Consts c, double dt, double* __restrict__ Vout,
+                                double* __restrict__ exch) {
+    extern __shared__ double sm[];
+    const int mb = blockIdx.x;
+    exchange_dev(links[mb], nets[mb], grids[mb], c, dt, Vout, exch, mb, sm);
+}
+
+// 1-D CFL rate over wet interior cells and whether any is wet (swe1d.py:253-262);
+// results valid in thread 0.  red: 64 doubles of shared memory.
+__device__ __forceinline__ void net_rate_dev(const Net& N, const Consts& c, double& rate_o, bool& wet_o, double* red) {
+    const Sec s{N.b, N.m, N.yb, N.ts};
+    double rate = 0.0, wet_any = 0.0;
+    for (int i = threadIdx.x; i < N.n_cells; i += blockDim.x) {
+        if (N.kind[i] > 1) continue;
+        const double A = N.A[i];
+        const double y = sec_depth(s, i, A);
+        if (!(y > c.h_dry)) continue;
+        wet_any = 1.0;
+        const double cc = sqrt(c.g * A / sec_top(s, i, y));
+        const double u = vel1d(c, s, i, A, N.Q[i]);
+        rate = fmax(rate, (fabs(u) + cc) / N.dx[i]);
+    }
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = (blockDim.x + 31) >> 5;
+    rate = warp_max(rate);
+    wet_any = warp_max(wet_any);
+    if (lane == 0) { red[warp * 2] = rate; red[warp * 2 + 1] = wet_any; }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        double r = red[0], w = red[1];
+        for (int k = 1; k < nw; ++k) { r = fmax(r, red[k * 2]); w = fmax(w, red[k * 2 + 1]); }
+        rate_o = r;
+        wet_o = w > 0.0;
+    }
+    __syncthreads();
 }
 
 }  // namespace his

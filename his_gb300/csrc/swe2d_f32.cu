@@ -10,4 +10,7 @@ int exchange_f32(his_links* l, const Consts& c, double dt, cudaStream_t s) { ret
 size_t stage_smem_bytes(int prec, int tx, int ty) {
     return prec == HIS_PREC_F64 ? stage_smem_impl<double>(tx, ty) : stage_smem_impl<float>(tx, ty);
 }
+int engine_enqueue_f32(his_engine* e, int n) { return engine_enqueue_impl<float>(e, n); }
+int engine_take_rate_f32(his_engine* e) { return engine_take_rate_impl<float>(e); }
+int engine_profile_f32(his_engine* e, int n, double* ms) { return engine_profile_impl<float>(e, n, ms); }
 }  // namespace his

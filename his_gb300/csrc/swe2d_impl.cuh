@@ -6,6 +6,7 @@
 #include "his_internal.h"
 #include "net1d_kernels.cuh"
 #include "swe2d_kernels.cuh"
+#include "engine_kernels.cuh"
 
 namespace his {
 
@@ -24,13 +25,13 @@ int launch_step_shape(his_grid* g, cudaStream_t s) {
     using G = TileGeom<R, TX, TY>;
     auto* grids = reinterpret_cast<const Grid<R>*>(g->d_grids);
     if (g->c.order == 2) {
-        stage_kernel<R, TX, TY, 1><<<g->n_tiles, G::NT, G::smem_bytes, s>>>(grids, g->d_tiles, g->d_params, g->c,
-                                                                            g->d_partials);
-        stage_kernel<R, TX, TY, 2><<<g->n_tiles, G::NT, G::smem_bytes, s>>>(grids, g->d_tiles, g->d_params, g->c,
-                                                                            g->d_partials);
+        stage_kernel<R, TX, TY, 1><<<g->n_tiles, G::NT, G::smem_bytes, s>>>(grids, g->d_tiles, g->d_params,
+                                                                            make_kc<R>(g->c), g->d_partials);
+        stage_kernel<R, TX, TY, 2><<<g->n_tiles, G::NT, G::smem_bytes, s>>>(grids, g->d_tiles, g->d_params,
+                                                                            make_kc<R>(g->c), g->d_partials);
     } else {
-        stage_kernel<R, TX, TY, 0><<<g->n_tiles, G::NT, G::smem_bytes, s>>>(grids, g->d_tiles, g->d_params, g->c,
-                                                                            g->d_partials);
+        stage_kernel<R, TX, TY, 0><<<g->n_tiles, G::NT, G::smem_bytes, s>>>(grids, g->d_tiles, g->d_params,
+                                                                            make_kc<R>(g->c), g->d_partials);
     }
     finalize_kernel<R><<<g->n, 32, 0, s>>>(grids, g->d_params, g->c, g->d_partials, g->d_out, 0);
     HIS_CK(cudaGetLastError());
@@ -40,7 +41,7 @@ int launch_step_shape(his_grid* g, cudaStream_t s) {
 template <class R, int TX, int TY>
 int launch_reduce_shape(his_grid* g, cudaStream_t s) {
     auto* grids = reinterpret_cast<const Grid<R>*>(g->d_grids);
-    cell_reduce_kernel<R, TX, TY><<<g->n_tiles, TX * TY, 0, s>>>(grids, g->d_tiles, g->c, g->d_partials);
+    cell_reduce_kernel<R, TX, TY><<<g->n_tiles, TX * TY, 0, s>>>(grids, g->d_tiles, make_kc<R>(g->c), g->d_partials);
     finalize_kernel<R><<<g->n, 32, 0, s>>>(grids, g->d_params, g->c, g->d_partials, g->d_out, 1);
     HIS_CK(cudaGetLastError());
     return HIS_OK;
@@ -89,6 +90,9 @@ int grid_init_impl(his_grid* g) {
         G.dy = d.dy;
         G.area = d.dx * d.dy;
         G.t0 = d.horton_t0;
+        G.rdx = R(d.dx);
+        G.rdy = R(d.dy);
+        G.rt0 = R(d.horton_t0);
         G.tiles_x = (d.nx + g->tx - 1) / g->tx;
         G.tiles_y = (d.ny + g->ty - 1) / g->ty;
         G.n_tiles = G.tiles_x * G.tiles_y;
@@ -104,6 +108,7 @@ int grid_init_impl(his_grid* g) {
         G.h1 = (R*)base; G.hu1 = (R*)(base + plane); G.hv1 = (R*)(base + 2 * plane);
         G.z = (const R*)d.z; G.n = (const R*)d.manning; G.S = (const R*)d.storage;
         G.f0 = (const R*)d.f0; G.fc = (const R*)d.fc; G.k = (const R*)d.k; G.rw = (const R*)d.rain_weight;
+        G.pk = (R*)d.peak_h; G.ps = (R*)d.peak_speed;
     }
     g->n_tiles = (int)tiles.size();
     HIS_CK(cudaMalloc(&g->d_grids, sizeof(Grid<R>) * n));
@@ -131,8 +136,8 @@ int exchange_impl(his_links* l, const Consts& c, double dt, cudaStream_t s) {
     if (l->smem > 48 * 1024)
         HIS_CK(cudaFuncSetAttribute(exchange_kernel<R>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)l->smem));
     exchange_kernel<R><<<l->n, 256, l->smem, s>>>(l->d_links, l->net->d_nets,
-                                                  reinterpret_cast<const Grid<R>*>(l->grid->d_grids), nullptr, c,
-                                                  dt, l->d_V, l->d_exch);
+                                                  reinterpret_cast<const Grid<R>*>(l->grid->d_grids), c, dt, l->d_V,
+                                                  l->d_exch);
     HIS_CK(cudaGetLastError());
     return HIS_OK;
 }
@@ -144,6 +149,122 @@ size_t stage_smem_impl(int tx, int ty) {
     if (tx == 64 && ty == 4) return TileGeom<R, 64, 4>::smem_bytes;
     if (tx == 16 && ty == 16) return TileGeom<R, 16, 16>::smem_bytes;
     return 0;
+}
+
+
+// One device-resident step for every member (see engine_kernels.cuh); the 1-D
+// substeps run on the side stream between a fork and a join event, concurrently
+// with the 2-D stages.
+template <class R, int TX, int TY>
+int eng_enqueue_shape(his_grid* g, his_engine* E, int n_steps) {
+    using G = TileGeom<R, TX, TY>;
+    auto* grids = reinterpret_cast<const Grid<R>*>(g->d_grids);
+    const Net* nets = E->net ? E->net->d_nets : nullptr;
+    const Lnk* links = E->links ? E->links->d_links : nullptr;
+    double* exch = E->links ? E->links->d_exch : nullptr;
+    for (int k = 0; k < n_steps; ++k) {
+        eng_pre_kernel<R><<<E->n, 256, E->pre_smem, E->s0>>>(E->d_em, g->d_params, grids, nets, links, g->c,
+                                                             E->d_netf, E->max_sub, exch);
+        if (E->net) {
+            HIS_CK(cudaEventRecord(E->ev_fork, E->s0));
+            HIS_CK(cudaStreamWaitEvent(E->s1, E->ev_fork, 0));
+            int rc = net_engine_launch(E, E->s1);
+            if (rc) return rc;
+            HIS_CK(cudaEventRecord(E->ev_join, E->s1));
+        }
+        if (g->c.order == 2) {
+            stage_kernel<R, TX, TY, 1><<<g->n_tiles, G::NT, G::smem_bytes, E->s0>>>(grids, g->d_tiles, g->d_params,
+                                                                                    make_kc<R>(g->c), g->d_partials);
+            stage_kernel<R, TX, TY, 2><<<g->n_tiles, G::NT, G::smem_bytes, E->s0>>>(grids, g->d_tiles, g->d_params,
+                                                                                    make_kc<R>(g->c), g->d_partials);
+        } else {
+            stage_kernel<R, TX, TY, 0><<<g->n_tiles, G::NT, G::smem_bytes, E->s0>>>(grids, g->d_tiles, g->d_params,
+                                                                                    make_kc<R>(g->c), g->d_partials);
+        }
+        if (E->net) HIS_CK(cudaStreamWaitEvent(E->s0, E->ev_join, 0));
+        eng_post_kernel<R><<<E->n, 32, 0, E->s0>>>(E->d_em, g->d_params, grids, g->c, g->d_partials,
+                                                   E->net ? E->d_vol1d : nullptr, g->d_out);
+        HIS_CK(cudaGetLastError());
+    }
+    return HIS_OK;
+}
+
+template <class R>
+int engine_enqueue_impl(his_engine* E, int n_steps) {
+    his_grid* g = E->grid;
+    HIS_TILE_DISPATCH(eng_enqueue_shape, R, g, E, n_steps);
+}
+
+template <class R>
+int engine_take_rate_impl(his_engine* E) {
+    // kernel attributes are set here, outside any stream capture
+    if (E->pre_smem > 48 * 1024)
+        HIS_CK(cudaFuncSetAttribute(eng_pre_kernel<R>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)E->pre_smem));
+    int rc = grid_reduce_impl<R>(E->grid, E->s0);
+    if (rc) return rc;
+    eng_take_rate_kernel<<<(E->n + 127) / 128, 128, 0, E->s0>>>(E->d_em, E->grid->d_out, E->n);
+    HIS_CK(cudaGetLastError());
+    return HIS_OK;
+}
+
+// Same step sequence as eng_enqueue_shape, uncaptured, with CUDA events around each
+// kernel class on its own stream; accumulates device milliseconds into ms[6].
+template <class R, int TX, int TY>
+int eng_profile_shape(his_grid* g, his_engine* E, int n_steps, double* ms) {
+    using G = TileGeom<R, TX, TY>;
+    auto* grids = reinterpret_cast<const Grid<R>*>(g->d_grids);
+    const Net* nets = E->net ? E->net->d_nets : nullptr;
+    const Lnk* links = E->links ? E->links->d_links : nullptr;
+    double* exch = E->links ? E->links->d_exch : nullptr;
+    cudaEvent_t ev[7];
+    for (auto& e : ev) HIS_CK(cudaEventCreate(&e));
+    int rc = HIS_OK;
+    for (int k = 0; k < n_steps && rc == HIS_OK; ++k) {
+        cudaEventRecord(ev[0], E->s0);
+        eng_pre_kernel<R><<<E->n, 256, E->pre_smem, E->s0>>>(E->d_em, g->d_params, grids, nets, links, g->c,
+                                                             E->d_netf, E->max_sub, exch);
+        cudaEventRecord(ev[1], E->s0);
+        if (E->net) {
+            cudaStreamWaitEvent(E->s1, ev[1], 0);
+            cudaEventRecord(ev[4], E->s1);
+            rc = net_engine_launch(E, E->s1);
+            cudaEventRecord(ev[5], E->s1);
+        }
+        if (g->c.order == 2) {
+            stage_kernel<R, TX, TY, 1><<<g->n_tiles, G::NT, G::smem_bytes, E->s0>>>(grids, g->d_tiles, g->d_params,
+                                                                                    make_kc<R>(g->c), g->d_partials);
+            cudaEventRecord(ev[2], E->s0);
+            stage_kernel<R, TX, TY, 2><<<g->n_tiles, G::NT, G::smem_bytes, E->s0>>>(grids, g->d_tiles, g->d_params,
+                                                                                    make_kc<R>(g->c), g->d_partials);
+        } else {
+            cudaEventRecord(ev[2], E->s0);
+            stage_kernel<R, TX, TY, 0><<<g->n_tiles, G::NT, G::smem_bytes, E->s0>>>(grids, g->d_tiles, g->d_params,
+                                                                                    make_kc<R>(g->c), g->d_partials);
+        }
+        cudaEventRecord(ev[3], E->s0);
+        if (E->net) cudaStreamWaitEvent(E->s0, ev[5], 0);
+        eng_post_kernel<R><<<E->n, 32, 0, E->s0>>>(E->d_em, g->d_params, grids, g->c, g->d_partials,
+                                                   E->net ? E->d_vol1d : nullptr, g->d_out);
+        cudaEventRecord(ev[6], E->s0);
+        cudaError_t ce = cudaEventSynchronize(ev[6]);
+        if (ce != cudaSuccess) { rc = cuda_fail(ce, "his_engine_profile"); break; }
+        float t;
+        cudaEventElapsedTime(&t, ev[0], ev[1]); ms[0] += t;
+        cudaEventElapsedTime(&t, ev[1], ev[2]); ms[1] += t;
+        cudaEventElapsedTime(&t, ev[2], ev[3]); ms[2] += t;
+        if (E->net) { cudaEventElapsedTime(&t, ev[4], ev[5]); ms[3] += t; }
+        cudaEventElapsedTime(&t, ev[3], ev[6]); ms[4] += t;
+        cudaEventElapsedTime(&t, ev[0], ev[6]); ms[5] += t;
+    }
+    for (auto& e : ev) cudaEventDestroy(e);
+    if (rc == HIS_OK) HIS_CK(cudaGetLastError());
+    return rc;
+}
+
+template <class R>
+int engine_profile_impl(his_engine* E, int n_steps, double* ms) {
+    his_grid* g = E->grid;
+    HIS_TILE_DISPATCH(eng_profile_shape, R, g, E, n_steps, ms);
 }
 
 }  // namespace his

@@ -26,29 +26,37 @@ struct TileGeom {
     static constexpr int XW = TX + 3, XH = TY + 2, NXF = XW * XH;      // x faces -1..TX+1, rows -1..TY
     static constexpr int YW = TX + 2, YH = TY + 3, NYF = YW * YH;      // y faces -1..TY+1, cols -1..TX
     static constexpr int TW = TX + 2, TH = TY + 2, NTH = TW * TH;      // theta ring
-    static constexpr int NRED = 10;
+    static constexpr int NRED = 11;
     static constexpr size_t smem_bytes =
         sizeof(R) * (4 * NR + 4 * NXF + 4 * NYF + NTH) + sizeof(double) * 32 * NRED + 16;
 };
 
 // Bed source and reconstructed bed of one cell along one axis (swe2d.py:220).
+// (float32: Zp - Zm is the in-cell bed slope d = sE - sH, see reconstruct())
 template <class R>
-__device__ __forceinline__ R bed_source(const Consts& c, R hm, R h0, R hp, R zm, R z0, R zp) {
+__device__ __forceinline__ R bed_source(const KC<R>& c, R hm, R h0, R hp, R zm, R z0, R zp) {
     R hmin = rmin(rmin(hm, h0), hp);
-    R ok = (hmin >= R(c.h_dry)) ? R(1) : R(0);
-    R em = hm + zm, e0 = h0 + z0, ep = hp + zp;
+    R ok = (hmin >= c.h_dry) ? R(1) : R(0);
     R sH = minmod(h0 - hm, hp - h0) * ok;
-    R sE = minmod(e0 - em, ep - e0) * ok;
     R Hm = h0 - R(0.5) * sH, Hp = h0 + R(0.5) * sH;
-    R Em = e0 - R(0.5) * sE, Ep = e0 + R(0.5) * sE;
-    R Zm = Em - Hm, Zp = Ep - Hp;
-    return R(-0.5 * c.g) * (Hm + Hp) * (Zp - Zm);
+    if constexpr (sizeof(R) == 8) {
+        R em = hm + zm, e0 = h0 + z0, ep = hp + zp;
+        R sE = minmod(e0 - em, ep - e0) * ok;
+        R Em = e0 - R(0.5) * sE, Ep = e0 + R(0.5) * sE;
+        R Zm = Em - Hm, Zp = Ep - Hp;
+        return c.nhg * (Hm + Hp) * (Zp - Zm);
+    } else {
+        // float32: the bed source plus the hydrostatic part of the face momentum fluxes,
+        // -g/2 (H+ + H-)(H+ - H- + Zp - Zm) = -g/2 (H+ + H-) sE (see riemann_wb)
+        R sE = minmod((h0 - hm) + (z0 - zm), (hp - h0) + (zp - z0)) * ok;
+        return c.nhg * (Hm + Hp) * sE;
+    }
 }
 
 // Load one halo-tile position: an interior cell, or the ghost that the x-sweep (for
 // cells outside in x) or the y-sweep (outside in y) would see (boundaries.py:81-128).
 template <class R>
-__device__ __forceinline__ void load_halo(const Consts& c, const Grid<R>& gd, const double* bcv, const R* __restrict__ H,
+__device__ __forceinline__ void load_halo(const KC<R>& c, const Grid<R>& gd, const R* bcv, const R* __restrict__ H,
                                           const R* __restrict__ HU, const R* __restrict__ HV, int gx, int gy, R& hh,
                                           R& uu, R& vv, R& zz) {
     const int nx = gd.nx, ny = gd.ny;
@@ -87,31 +95,50 @@ __device__ __forceinline__ void load_halo(const Consts& c, const Grid<R>& gd, co
     R hg, ung, utg;
     if (kind == BC_CLOSED) { hg = h0; ung = -un; utg = ut; }
     else if (kind == BC_TRANSMISSIVE) { hg = h0; ung = un; utg = ut; }
-    else if (kind == BC_STAGE) stage_ghost(c, R(bcv[side]), h0, un, ut, z0, hg, ung, utg);
-    else discharge_ghost(c, R(bcv[side]), h0, hg, ung, utg);
+    else if (kind == BC_STAGE) stage_ghost(c, bcv[side], h0, un, ut, z0, hg, ung, utg);
+    else discharge_ghost(c, bcv[side], h0, hg, ung, utg);
     hh = hg;
     zz = z0;
     if (alongx) { uu = sgn * ung; vv = utg; }
     else { vv = sgn * ung; uu = utg; }
 }
 
-template <int NV>
-__device__ __forceinline__ void block_reduce_store(double (&v)[NV], const bool* is_max, double* red, double* out,
+template <class T>
+__device__ __forceinline__ T warp_sum_t(T v) {
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+    return v;
+}
+template <class T>
+__device__ __forceinline__ T warp_max_t(T v) {
+    for (int o = 16; o > 0; o >>= 1) {
+        T w = __shfl_down_sync(0xffffffffu, v, o);
+        v = w > v ? w : v;
+    }
+    return v;
+}
+
+// Block reduction of NV per-thread values in the compute type T: within each warp by
+// shuffles, then across warps by lane j of warp 0 for value j (warps in order), which
+// converts its result once and writes it to out[slots[j]] (the float64 tile partial).
+template <int NV, class T>
+__device__ __forceinline__ void block_reduce_store(T (&v)[NV], const bool* is_max, T* red, double* out,
                                                    const int* slots, int nthreads) {
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = nthreads >> 5;
 #pragma unroll
-    for (int j = 0; j < NV; ++j) v[j] = is_max[j] ? warp_max(v[j]) : warp_sum(v[j]);
+    for (int j = 0; j < NV; ++j) v[j] = is_max[j] ? warp_max_t(v[j]) : warp_sum_t(v[j]);
     if (lane == 0) {
 #pragma unroll
         for (int j = 0; j < NV; ++j) red[warp * NV + j] = v[j];
     }
     __syncthreads();
-    if (threadIdx.x == 0) {
-        for (int j = 0; j < NV; ++j) {
-            double a = red[j];
-            for (int w = 1; w < nw; ++w) a = is_max[j] ? fmax(a, red[w * NV + j]) : a + red[w * NV + j];
-            out[slots[j]] = a;
+    if (warp == 0 && lane < NV) {
+        const bool mx = is_max[lane];
+        T a = red[lane];
+        for (int w = 1; w < nw; ++w) {
+            const T b = red[w * NV + lane];
+            a = mx ? (b > a ? b : a) : a + b;
         }
+        out[slots[lane]] = (double)a;
     }
 }
 
@@ -119,7 +146,7 @@ __device__ __forceinline__ void block_reduce_store(double (&v)[NV], const bool* 
 template <class R, int TX, int TY, int STAGE>
 __global__ void __launch_bounds__(TX * TY) stage_kernel(const Grid<R>* __restrict__ grids,
                                                          const TileRef* __restrict__ tiles,
-                                                         const StepParams* __restrict__ params, Consts c,
+                                                         const StepParams* __restrict__ params, const KC<R> c,
                                                          double* __restrict__ partials) {
     using G = TileGeom<R, TX, TY>;
     extern __shared__ __align__(16) unsigned char smem_raw[];
@@ -136,7 +163,8 @@ __global__ void __launch_bounds__(TX * TY) stage_kernel(const Grid<R>* __restric
     R* yF2R = yF2L + G::NYF;
     R* yF3 = yF2R + G::NYF;
     R* thS = yF3 + G::NYF;
-    double* red = reinterpret_cast<double*>((reinterpret_cast<uintptr_t>(thS + G::NTH) + 15) & ~uintptr_t(15));
+    R* red = reinterpret_cast<R*>((reinterpret_cast<uintptr_t>(thS + G::NTH) + 15) & ~uintptr_t(15));
+    __shared__ R bcv[4];
 
     const TileRef tr = tiles[blockIdx.x];
     const Grid<R>& gd = grids[tr.member];
@@ -144,8 +172,9 @@ __global__ void __launch_bounds__(TX * TY) stage_kernel(const Grid<R>* __restric
     if (!pr.active) return;
     const int nx = gd.nx, ny = gd.ny, x0 = tr.x0, y0 = tr.y0;
     const int tid = threadIdx.x;
-    const R dt = R(pr.dt);
-    const double* bcv = STAGE == 2 ? pr.bc1 : pr.bc0;
+    const R dt = par_dt<R>(pr);
+    if (tid < 4) bcv[tid] = par_bc<R>(pr, STAGE == 2, tid);
+    __syncthreads();
     const R* __restrict__ H = STAGE == 2 ? gd.h1 : gd.h;
     const R* __restrict__ HU = STAGE == 2 ? gd.hu1 : gd.hu;
     const R* __restrict__ HV = STAGE == 2 ? gd.hv1 : gd.hv;
@@ -195,7 +224,7 @@ __global__ void __launch_bounds__(TX * TY) stage_kernel(const Grid<R>* __restric
     __syncthreads();
 
     // ---- C: positivity-limiter theta on the tile plus a one-cell ring (swe2d.py:259-264)
-    const R rdx = R(gd.dx), rdy = R(gd.dy);
+    const R rdx = gd.rdx, rdy = gd.rdy;
     for (int p = tid; p < G::NTH; p += G::NT) {
         int ti = p / G::TW, tj = p - ti * G::TW;
         int x = tj - 1, y = ti - 1;
@@ -214,7 +243,12 @@ __global__ void __launch_bounds__(TX * TY) stage_kernel(const Grid<R>* __restric
     __syncthreads();
 
     // ---- D: update of the tile's own cells
-    double acc_clip = 0, xin = 0, xout = 0, yin = 0, yout = 0, infil = 0, rainw = 0, rate = 0, hsum = 0, ssum = 0;
+    // per-cell contributions in the compute type; the block sums them per warp in R and
+    // across warps (and the finalize kernel across tiles) in float64
+    R acc_clip = 0, xin = 0, xout = 0, yin = 0, yout = 0, infil = 0, rainw = 0, rate = 0, hsum = 0, ssum = 0;
+    R hmax = 0;
+    const R rdt = par_rain<R>(pr) * dt;
+    const R tt = clamp0(par_t<R>(pr) - gd.rt0);
     const int x = tid % TX, y = tid / TX;
     const int gx = x0 + x, gy = y0 + y;
     if (gx < nx && gy < ny) {
@@ -242,10 +276,10 @@ __global__ void __launch_bounds__(TX * TY) stage_kernel(const Grid<R>* __restric
             b2 = b2 + scy / rdy;
         }
         const R dh = a1 + b1, dhu = a2 + b3, dhv = a3 + b2;
-        if (gx == 0) { xin += (double)relu(F1w); xout += (double)relu(-F1w); }
-        if (gx == nx - 1) { xin += (double)relu(-F1e); xout += (double)relu(F1e); }
-        if (gy == 0) { yin += (double)relu(G1s); yout += (double)relu(-G1s); }
-        if (gy == ny - 1) { yin += (double)relu(-G1n); yout += (double)relu(G1n); }
+        if (gx == 0) { xin += relu(F1w); xout += relu(-F1w); }
+        if (gx == nx - 1) { xin += relu(-F1e); xout += relu(F1e); }
+        if (gy == 0) { yin += relu(G1s); yout += relu(-G1s); }
+        if (gy == ny - 1) { yin += relu(-G1n); yout += relu(G1n); }
 
         const size_t i = (size_t)gy * nx + gx;
         R hn, hun, hvn;
@@ -260,7 +294,7 @@ __global__ void __launch_bounds__(TX * TY) stage_kernel(const Grid<R>* __restric
             hvn = gd.hv[i] + dt * dhv;
         }
         R neg = clamp0(-hn);
-        acc_clip = (double)neg;
+        acc_clip = neg;
         hn = hn + neg;
         if (STAGE == 1) {
             gd.h1[i] = hn; gd.hu1[i] = hun; gd.hv1[i] = hvn;
@@ -268,16 +302,14 @@ __global__ void __launch_bounds__(TX * TY) stage_kernel(const Grid<R>* __restric
             // ---- sources after the RK update (swe2d.py:330-360)
             R sf = gd.S ? gd.sf[i] : R(0);
             R icum = gd.f0 ? gd.ic[i] : R(0);
-            const R rdt = R(pr.rain) * dt;
             if (gd.rw) {
                 R add = rdt * gd.rw[i];
                 hn = hn + add;
-                rainw = (double)add;
+                rainw = add;
             } else {
                 hn = hn + rdt;
             }
             if (gd.f0) {
-                R tt = clamp0(R(pr.t) - R(gd.t0));
                 R f0 = gd.f0[i], fc = gd.fc[i], kk = gd.k[i];
                 R rate_f = fc + (f0 - fc) * rexp(-kk * tt);
                 R pot = rate_f * dt;
@@ -294,7 +326,7 @@ __global__ void __launch_bounds__(TX * TY) stage_kernel(const Grid<R>* __restric
                     taken = taken + tks;
                 }
                 icum = icum + taken;
-                infil = (double)taken;
+                infil = taken;
                 gd.ic[i] = icum;
             }
             if (gd.S) {
@@ -312,47 +344,50 @@ __global__ void __launch_bounds__(TX * TY) stage_kernel(const Grid<R>* __restric
             R u, v;
             kp_velocity(c, hn, hun, hvn, u, v);
             R speed = dsqrt(u * u + v * v);
-            R hf = rmax(hn, R(c.h_dry));
+            R hf = rmax(hn, c.h_dry);
             R nm = gd.n[i];
-            R denom = R(1) + dt * R(c.g) * nm * nm * speed / pow43(hf);
+            R denom = R(1) + dt * c.g * nm * nm * speed / pow43(hf);
             u = u / denom;
             v = v / denom;
-            bool wet = hn >= R(c.h_dry);
+            bool wet = hn >= c.h_dry;
             hun = wet ? hn * u : R(0);
             hvn = wet ? hn * v : R(0);
             gd.h[i] = hn; gd.hu[i] = hun; gd.hv[i] = hvn;
+            if (gd.pk) gd.pk[i] = rmax(gd.pk[i], hn);
+            if (gd.ps) gd.ps[i] = rmax(gd.ps[i], wet ? dsqrt(u * u + v * v) : R(0));
             // ---- CFL rate of the new state for the next step (swe2d.py:179-184)
             R u2, v2;
             kp_velocity(c, hn, hun, hvn, u2, v2);
-            R cw = dsqrt(R(c.g) * hn);
-            R r = hn > R(c.h_dry) ? (fabs(u2) + cw) / rdx + (fabs(v2) + cw) / rdy : R(0);
-            rate = (double)r;
-            hsum = (double)hn;
-            ssum = (double)sf;
+            R cw = dsqrt(c.g * hn);
+            R r = hn > c.h_dry ? (fabs(u2) + cw) / rdx + (fabs(v2) + cw) / rdy : R(0);
+            rate = r;
+            hsum = hn;
+            ssum = sf;
+            hmax = hn;
         }
     }
     __syncthreads();
     double* out = partials + (size_t)blockIdx.x * NPART;
     if (STAGE == 1) {
-        double v[5] = {acc_clip, xin, xout, yin, yout};
+        R v[5] = {acc_clip, xin, xout, yin, yout};
         const bool mx[5] = {false, false, false, false, false};
         const int sl[5] = {P_CLIP1, P_XIN1, P_XOUT1, P_YIN1, P_YOUT1};
         block_reduce_store<5>(v, mx, red, out, sl, G::NT);
     } else {
         const int b = STAGE == 2 ? P_CLIP2 : P_CLIP1;
-        double v[10] = {acc_clip, xin, xout, yin, yout, infil, rainw, rate, hsum, ssum};
-        const bool mx[10] = {false, false, false, false, false, false, false, true, false, false};
-        const int sl[10] = {b, b + 1, b + 2, b + 3, b + 4, P_INFIL, P_RAINW, P_RATE, P_HSUM, P_SSUM};
-        block_reduce_store<10>(v, mx, red, out, sl, G::NT);
+        R v[11] = {acc_clip, xin, xout, yin, yout, infil, rainw, rate, hsum, ssum, hmax};
+        const bool mx[11] = {false, false, false, false, false, false, false, true, false, false, true};
+        const int sl[11] = {b, b + 1, b + 2, b + 3, b + 4, P_INFIL, P_RAINW, P_RATE, P_HSUM, P_SSUM, P_HMAX};
+        block_reduce_store<11>(v, mx, red, out, sl, G::NT);
     }
 }
 
 // Per-tile CFL rate, surface and retained water of the current state (no halo).
 template <class R, int TX, int TY>
 __global__ void __launch_bounds__(TX * TY) cell_reduce_kernel(const Grid<R>* __restrict__ grids,
-                                                               const TileRef* __restrict__ tiles, Consts c,
+                                                               const TileRef* __restrict__ tiles, const KC<R> c,
                                                                double* __restrict__ partials) {
-    __shared__ double red[32 * 3];
+    __shared__ double red[32 * 3];   // volumes are summed in float64 (this kernel is not on the step path)
     const TileRef tr = tiles[blockIdx.x];
     const Grid<R>& gd = grids[tr.member];
     const int x = threadIdx.x % TX, y = threadIdx.x / TX;
@@ -362,8 +397,8 @@ __global__ void __launch_bounds__(TX * TY) cell_reduce_kernel(const Grid<R>* __r
         size_t i = (size_t)gy * gd.nx + gx;
         R h = gd.h[i], u, v;
         kp_velocity(c, h, gd.hu[i], gd.hv[i], u, v);
-        R cw = dsqrt(R(c.g) * h);
-        R r = h > R(c.h_dry) ? (fabs(u) + cw) / R(gd.dx) + (fabs(v) + cw) / R(gd.dy) : R(0);
+        R cw = dsqrt(c.g * h);
+        R r = h > c.h_dry ? (fabs(u) + cw) / gd.rdx + (fabs(v) + cw) / gd.rdy : R(0);
         rate = (double)r;
         hs = (double)h;
         ss = gd.sf ? (double)gd.sf[i] : 0.0;
@@ -389,10 +424,10 @@ __global__ void finalize_kernel(const Grid<R>* __restrict__ grids, const StepPar
     for (int t = lane; t < gd.n_tiles; t += 32) {
         const double* p = partials + (size_t)(gd.tile0 + t) * NPART;
 #pragma unroll
-        for (int j = 0; j < NPART; ++j) s[j] = (j == P_RATE) ? fmax(s[j], p[j]) : s[j] + p[j];
+        for (int j = 0; j < NPART; ++j) s[j] = (j == P_RATE || j == P_HMAX) ? fmax(s[j], p[j]) : s[j] + p[j];
     }
 #pragma unroll
-    for (int j = 0; j < NPART; ++j) s[j] = (j == P_RATE) ? warp_max(s[j]) : warp_sum(s[j]);
+    for (int j = 0; j < NPART; ++j) s[j] = (j == P_RATE || j == P_HMAX) ? warp_max(s[j]) : warp_sum(s[j]);
     if (lane != 0) return;
     double* o = out + (size_t)m * 8;
     o[5] = s[P_RATE];

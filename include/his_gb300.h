@@ -57,6 +57,9 @@ typedef struct his_grid_desc {
     double horton_t0;
     void *h, *hu, *hv, *s_filled, *infil_cum;
     const void *z, *manning, *storage, *f0, *fc, *k, *rain_weight;
+    /* optional running maxima over every step (NULL = off): surface depth and speed
+     * (replaces the peak fields built from snapshots, hydrointel/api.py:238-241) */
+    void *peak_h, *peak_speed;
 } his_grid_desc;
 
 /* Per-member forcing of one step: dt, step-start time, rain rate (m/s) and edge
@@ -160,6 +163,65 @@ int32_t his_exchange(his_links* links, const his_solver_cfg* cfg, double dt, dou
  * n_members x 2 (2-D -> 1-D, 1-D -> 2-D), host out, synchronises.  reset != 0 zeroes
  * them afterwards.  Replaces the exchange tallies of hydrointel/solver/coupling.py:210-211. */
 int32_t his_links_exchanged(his_links* links, double* totals, int32_t reset, void* stream);
+
+/* ------------------------------------------------------------------ engine */
+/* Per-member forcing of the device-resident engine (host arrays copied at creation):
+ * piecewise-constant rain blocks (m/s) from rain_t0 in blocks of rain_step seconds;
+ * a harmonic tide base + sum amp cos(w (t + shift) - phase) (used by stage edges and
+ * the 1-D stage end); a linearly interpolated inflow hydrograph (m^3/s, used by the
+ * 1-D inflow end); and per 2-D edge a value source: 0 constant edge_val, 1 the
+ * tide, 2 inflow x edge_val (a discharge per unit width).
+ * Replaces hydrointel/engine.py:104-166 (BatchForcing), hyetograph.py:42-46,
+ * tide.py:29-31, catchment.py:32-40. */
+typedef struct his_forcing_desc {
+    double t0, t_end;
+    double rain_t0, rain_step;
+    int32_t rain_n, tide_on;
+    const double* rain;
+    int32_t tide_n, q_n;
+    double tide_base, tide_shift;
+    double tide_amp[4], tide_w[4], tide_phase[4];
+    double q_t0, q_step;
+    const double* q;
+    int32_t edge_src[4];
+    double edge_val[4];
+} his_forcing_desc;
+
+/* What the host reads back per member. status: 0 running, 1 done, 2 non-finite
+ * state, 3 implausible state (2-D depth > 10 m), 4 more 1-D substeps than allowed.
+ * acc: float64 volume totals (rain, infiltration, bnd2d_in, bnd2d_out, bnd1d_in,
+ * bnd1d_out, clip) in m^3, in the reference's mass-balance terms. */
+typedef struct his_member_report {
+    double t, dt_last, dt_min, dt_max, rate;
+    int64_t steps;
+    int32_t status, n_sub_max, n_dt_clamped, pad;
+    double acc[7];
+} his_member_report;
+
+typedef struct his_engine his_engine;
+
+/* Device-resident coupled time loop over a grid set and (optionally) a network set
+ * with links: every member advances with its own CFL dt until its t_end, forcing,
+ * exchange, 1-D substeps, 2-D step and accounting all on the device, captured as
+ * CUDA graphs of graph_steps steps (0 = default).  max_sub bounds the 1-D substeps
+ * per step (0 = 64).  Replaces the per-step host loop of
+ * hydrointel/solver/coupling.py:201-286 (CoupledEngine.step / run). */
+int32_t his_engine_create(his_grid* grid, his_net* net, his_links* links, int32_t n_members,
+                          const his_forcing_desc* forcing, int32_t max_sub, int32_t graph_steps, his_engine** out);
+int32_t his_engine_destroy(his_engine* engine);
+
+/* Enqueue n_steps steps of every running member on `stream` (asynchronous). */
+int32_t his_engine_advance(his_engine* engine, int32_t n_steps, void* stream);
+
+/* Per-member reports (host out, n_members; synchronises). */
+int32_t his_engine_report(his_engine* engine, his_member_report* reports, void* stream);
+
+/* Run n_steps steps without graphs, bracketing each kernel class with CUDA events on
+ * the stream it is launched on, and return the summed device milliseconds per class:
+ * ms[0] pre (dt, exchange, forcing), ms[1] 2-D stage 1, ms[2] 2-D stage 2 + sources,
+ * ms[3] 1-D substeps, ms[4] post (accounting), ms[5] whole steps.  Synchronises.
+ * No reference counterpart: the measurement hook of the roofline report. */
+int32_t his_engine_profile(his_engine* engine, int32_t n_steps, double* ms, void* stream);
 
 #ifdef __cplusplus
 }

@@ -129,3 +129,30 @@ def cuda_overtop(fx: dict, dtype=None, cfg: SolverConfig | None = None):
     one = SWE1D(overtop_network(CH), p.cfg, inflow=p.inflow, stage=p.stage)
     links = build_links(one, two)
     return one, two, links, p
+
+
+def oracle_from_storm(storm, cfg: SolverConfig | None = None):
+    """The oracle's coupled engine for a synthetic storm (same fields, network, links, forcing)."""
+    from oracle.oracle import OracleCoupled, OracleLinks, OracleSWE1D, OracleSWE2D
+    from his_gb300.assembly import storm_bcs
+    from his_gb300.topology import build_topology, sections
+    from his_gb300.workloads import bank_links, normal_depth
+    cfg = cfg or SolverConfig(slot_width_frac=storm.slot_width_frac)
+    ter = storm.terrain
+    two = OracleSWE2D(ter.z, np.broadcast_to(np.asarray(storm.manning, float), ter.z.shape), ter.dx, cfg,
+                      storm_bcs(storm), storage=storm.storage, horton=storm.horton)
+    two.set_state(storm.h0())
+    f = storm.forcing
+    if storm.network is None:
+        return OracleCoupled(two, None, None, cfg, rain=f.rain_rate)
+    tp = build_topology(storm.network)
+    one = OracleSWE1D(tp, cfg, inflow=f.inflow, stage=f.tide)
+    sec = sections(tp, cfg.slot_width_frac)
+    y = np.maximum(np.maximum(tp.z + normal_depth(tp, sec, f.inflow(0.0)), f.tide(0.0)) - tp.z, 0.0)
+    yt = np.minimum(y, sec["yb"])
+    one.A[0] = yt * (sec["b"] + sec["m"] * yt) + sec["ts"] * np.maximum(y - sec["yb"], 0.0)
+    cell1d, cells2d, length = bank_links(ter, tp)
+    uniq, inv = np.unique(cells2d, return_inverse=True)
+    links = OracleLinks(cell1d, tp.zbank[cell1d], np.full(len(cell1d), length), ter.z.reshape(-1)[cells2d], inv,
+                        uniq)
+    return OracleCoupled(two, one, links, cfg, rain=f.rain_rate)

@@ -1,0 +1,157 @@
+"""The CUDA engine on the synthetic workloads: spec parity with the oracle, lake at
+rest, mass balance, per-member time steps, batched == solo, float32 production form."""
+import numpy as np
+import pytest
+import torch
+
+import harness as H
+
+pytestmark = pytest.mark.gpu
+
+
+def _np(t):
+    return t.detach().double().cpu().numpy()
+
+
+def test_plain_small_1000_steps_match_oracle():
+    """Plain float64 method, 100x81 @ 80 m coupled storm: after 1000 steps driven by the
+    oracle's own CFL sequence, max |dh| <= 1e-9 m and max |d(hu, hv)| <= 1e-9 m^2/s."""
+    from his_gb300 import workloads as W
+    from his_gb300.assembly import build_engine
+    storm = W.plain_small()
+    eng = build_engine(storm)
+    orc = H.oracle_from_storm(storm)
+    t = 0.0
+    for k in range(1000):
+        dt = min(orc.two.max_dt(), storm.t_end - t)
+        n_sub = max(1, int(np.ceil(dt / orc.one.max_dt() - 1e-9)))
+        orc.step(t, storm.t_end, dt=dt, n_sub=n_sub)
+        t = eng.step(t, storm.t_end, dt=dt, n_sub=n_sub)
+    dh = H.max_abs(_np(eng.two.h), orc.two.h[0])
+    dhu = H.max_abs(_np(eng.two.hu), orc.two.hu[0])
+    dhv = H.max_abs(_np(eng.two.hv), orc.two.hv[0])
+    dA = H.max_abs(_np(eng.one.A), orc.one.A[0])
+    print(f"after 1000 steps (t = {t:.1f} s): |dh| {dh:.3e} m, |dhu| {dhu:.3e}, |dhv| {dhv:.3e}, |dA| {dA:.3e}")
+    assert dh <= 1e-9 and dhu <= 1e-9 and dhv <= 1e-9
+    assert dA <= 1e-8
+    src = eng.mb.sources()
+    for term, v in orc.acc.items():
+        assert src[term] == pytest.approx(float(v[0]), rel=1e-9, abs=1e-6), term
+    assert eng.mb.check(eng.total_volume(), t, record=False) < 1e-3
+
+
+@pytest.mark.parametrize("dtype,tol", [(torch.float64, 1e-10), (torch.float32, 1e-5)])
+def test_lake_at_rest_over_synthetic_dem(dtype, tol):
+    """Still water over the full-resolution seeded DEM, partly dry, closed edges: after 500
+    steps the spurious velocity stays below 1e-10 m/s (float64; 1e-5 for float32)."""
+    from his_gb300 import workloads as W
+    from his_gb300.boundaries import all_edges
+    from his_gb300.config import SolverConfig
+    from his_gb300.swe2d import SWE2D
+    ter = W.make_terrain(400, 325, 20.0, 24, "plain_full", "triple")
+    eta0 = float(np.quantile(ter.z, 0.6))
+    sim = SWE2D(ter.z, 0.035, ter.dx, SolverConfig(), all_edges("closed"), dtype=dtype)
+    sim.set_level(eta0)
+    wet0 = _np(sim.h) > 0
+    for _ in range(500):
+        sim.step(sim.max_dt(), 0.0, 0.0)
+    u, v = sim.velocities(sim.h, sim.hu, sim.hv)
+    umax = max(float(u.abs().max()), float(v.abs().max()))
+    deta = float(np.abs((_np(sim.h) + ter.z - eta0) * wet0).max())
+    speed = np.hypot(_np(u), _np(v))
+    j, i = np.unravel_index(np.argmax(speed), speed.shape)
+    h = _np(sim.h)
+    print(f"{dtype}: wet fraction {wet0.mean():.2f}, max |u|,|v| {umax:.3e} m/s at depth {h[j, i]:.4g} m "
+          f"(cell {j},{i}), 99th pct speed {np.quantile(speed[wet0], 0.99):.3e}, "
+          f"max |eta - eta0| {deta:.3e} m")
+    assert umax < tol and deta < tol
+
+
+def test_engine_matches_dropin_path_fp64():
+    """The device-resident engine (dt, forcing and accounting on the GPU, graphs) takes the
+    same steps as the drop-in path on the plain small storm."""
+    from his_gb300 import workloads as W
+    from his_gb300.assembly import build_engine
+    from his_gb300.config import SolverConfig
+    from his_gb300.engine import FloodEngine
+    storm = W.plain_small()
+    fe = FloodEngine([storm], SolverConfig(slot_width_frac=storm.slot_width_frac), precision="fp64",
+                     graph_steps=8)
+    eng = build_engine(storm)
+    t = 0.0
+    for _ in range(100):
+        t = eng.step(t, storm.t_end)
+    fe.advance(100)
+    r = fe.reports()[0]
+    assert r.steps == 100 and r.t == pytest.approx(t, rel=1e-12)
+    assert H.max_abs(_np(fe.h[0]), _np(eng.two.h)) <= 1e-12
+    assert H.max_abs(_np(fe.A[0]), _np(eng.one.A)) <= 1e-10
+    src = eng.mb.sources()
+    for j, term in enumerate(("rain", "infiltration", "bnd2d_in", "bnd2d_out", "bnd1d_in", "bnd1d_out", "clip")):
+        assert r.acc[j] == pytest.approx(src[term], rel=1e-9, abs=1e-6), term
+
+
+def test_batched_member_is_bit_identical_to_solo():
+    """Per-member dt: a member advanced inside an uneven batch equals the same storm alone,
+    bit for bit (float32 production form)."""
+    from his_gb300 import workloads as W
+    from his_gb300.engine import FloodEngine
+    storms = [W.uneven_member(f"solo-vs-batch/{k}", k % 3, 1800.0 + 600.0 * k) for k in range(4)]
+    batch = FloodEngine(storms, precision="fp32")
+    solo = FloodEngine([storms[2]], precision="fp32")
+    batch.advance(150)
+    solo.advance(150)
+    rb, rs = batch.reports()[2], solo.reports()[0]
+    assert rb.steps == rs.steps == 150 and rb.t == rs.t
+    assert torch.equal(batch.h[2], solo.h[0]) and torch.equal(batch.hu[2], solo.hu[0])
+    assert torch.equal(batch.A[2], solo.A[0]) and torch.equal(batch.Q[2], solo.Q[0])
+    assert list(rb.acc) == list(rs.acc)
+    # members really take different steps
+    dts = {round(r.dt_last, 9) for r in batch.reports()}
+    assert len(dts) > 1
+
+
+@pytest.mark.parametrize("precision", ["fp64", "fp32"])
+def test_full_storm_mass_balance(precision):
+    """The plain small storm run to its end through the engine: per-member mass error < 1e-3."""
+    from his_gb300 import workloads as W
+    from his_gb300.config import SolverConfig
+    from his_gb300.engine import FloodEngine
+    storm = W.plain_small()
+    fe = FloodEngine([storm], SolverConfig(slot_width_frac=storm.slot_width_frac), precision=precision)
+    reps = fe.run(chunk=512)
+    assert reps[0].status == 1, f"member ended with status {reps[0].status}"
+    errs = fe.assert_mass_ok()
+    res = fe.results()[0]
+    print(f"{precision}: {res.steps} steps, dt {res.dt_min:.3f}..{res.dt_max:.3f} s, mass error {errs[0]:.3e}, "
+          f"sources {res.sources}")
+    assert res.sources["rain"] > 0 and res.sources["bnd2d_out"] >= 0
+
+
+def test_fp32_production_form_against_fp64():
+    """Production form (float32 state and fluxes, float64 accumulators) against the plain
+    float64 method on the same storm run to its end: peak-depth RMSE <= 1 cm, mass
+    error < 1e-3, and the volume error reported."""
+    from his_gb300 import workloads as W
+    from his_gb300.config import SolverConfig
+    from his_gb300.engine import FloodEngine
+    storm = W.plain_small()
+    runs = {}
+    for prec in ("fp64", "fp32"):
+        fe = FloodEngine([storm], SolverConfig(slot_width_frac=storm.slot_width_frac), precision=prec,
+                         track_peaks=True)
+        reps = fe.run(chunk=512)
+        assert reps[0].status == 1
+        fe.assert_mass_ok()
+        runs[prec] = (fe, fe.results()[0])
+    p64 = _np(runs["fp64"][0].peak_h[0])
+    p32 = _np(runs["fp32"][0].peak_h[0])
+    wet = (p64 > 1e-3) | (p32 > 1e-3)
+    rmse = float(np.sqrt(np.mean((p32 - p64)[wet] ** 2)))
+    dmax = float(np.abs(p32 - p64).max())
+    r64, r32 = runs["fp64"][1], runs["fp32"][1]
+    vol_err = abs(r32.volume - r64.volume) / max(r64.volume, 1.0)
+    print(f"peak depth: RMSE {rmse * 1e3:.3f} mm, max {dmax * 1e3:.2f} mm over {int(wet.sum())} wet cells; "
+          f"final volume rel. error {vol_err:.2e}; steps fp64 {r64.steps} fp32 {r32.steps}")
+    assert rmse <= 0.01
+    assert vol_err < 1e-3
