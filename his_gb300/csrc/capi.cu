@@ -19,14 +19,9 @@ int cuda_fail(cudaError_t e, const char* what) {
     return HIS_ERR_CUDA;
 }
 
-const TileShape kTileShapes[] = {{32, 8}, {32, 16}, {64, 4}, {16, 16}};
-const int kNumTileShapes = 4;
-
-bool tile_supported(int tx, int ty) {
-    for (int i = 0; i < kNumTileShapes; ++i)
-        if (kTileShapes[i].tx == tx && kTileShapes[i].ty == ty) return true;
-    return false;
-}
+// Work decomposition of the 2-D kernels: strips of at most tx columns (a CTA of 64
+// threads up to 58 columns, 128 up to 122), chunks of ty rows.
+bool tile_supported(int tx, int ty) { return tx >= 1 && tx <= 122 && ty >= 1 && ty <= 1 << 20; }
 
 static Consts to_consts(const his_solver_cfg* c) {
     Consts k{};
@@ -90,8 +85,9 @@ int32_t his_grid_create(int32_t precision, const his_solver_cfg* cfg, int32_t n_
     if (rc) return rc;
     if (precision != HIS_PREC_F64 && precision != HIS_PREC_F32) return bad("precision must be 0 (f64) or 1 (f32)");
     if (n_members <= 0 || !grids) return bad("need at least one grid member");
-    if (tile_x == 0 && tile_y == 0) { tile_x = 32; tile_y = 8; }
-    if (!tile_supported(tile_x, tile_y)) return bad("unsupported tile shape");
+    if (tile_x == 0) tile_x = 58;
+    if (tile_y == 0) tile_y = 48;
+    if (!tile_supported(tile_x, tile_y)) return bad("unsupported work decomposition (strip width 1..122, rows >= 1)");
     for (int m = 0; m < n_members; ++m) {
         const his_grid_desc& d = grids[m];
         std::string who = "member " + std::to_string(m) + ": ";
@@ -110,6 +106,7 @@ int32_t his_grid_create(int32_t precision, const his_solver_cfg* cfg, int32_t n_
     g->c = to_consts(cfg);
     g->n = n_members;
     g->tx = tile_x;
+    g->nt = tile_x <= 58 ? 64 : 128;
     g->ty = tile_y;
     g->desc.assign(grids, grids + n_members);
     cudaGetDevice(&g->device);

@@ -12,7 +12,7 @@
 //             float64 accumulators, t += dt, plausibility (coupling.py:213-227, :169-192)
 #pragma once
 #include "net1d_kernels.cuh"
-#include "swe2d_kernels.cuh"
+#include "swe2d_strip.cuh"
 
 namespace his {
 

@@ -12,7 +12,7 @@
 struct his_grid {
     int prec = 0;
     his::Consts c{};
-    int n = 0, tx = 32, ty = 8, device = 0;
+    int n = 0, tx = 58, ty = 48, nt = 64, device = 0;   // strip width, rows per chunk, threads per CTA
     std::vector<his_grid_desc> desc;
     std::vector<int> tile0, ntile;
     void* d_grids = nullptr;                 // his::Grid<R>[n]
@@ -80,10 +80,6 @@ int cuda_fail(cudaError_t e, const char* what);
         if (e_ != cudaSuccess) return his::cuda_fail(e_, #call); \
     } while (0)
 
-// Tile shapes compiled into the library (TX, TY)
-struct TileShape { int tx, ty; };
-extern const TileShape kTileShapes[];
-extern const int kNumTileShapes;
 bool tile_supported(int tx, int ty);
 
 // precision-specific entry points (swe2d_f64.cu / swe2d_f32.cu)

@@ -8,7 +8,9 @@ int grid_step_f32(his_grid* g, cudaStream_t s) { return grid_step_impl<float>(g,
 int grid_reduce_f32(his_grid* g, cudaStream_t s) { return grid_reduce_impl<float>(g, s); }
 int exchange_f32(his_links* l, const Consts& c, double dt, cudaStream_t s) { return exchange_impl<float>(l, c, dt, s); }
 size_t stage_smem_bytes(int prec, int tx, int ty) {
-    return prec == HIS_PREC_F64 ? stage_smem_impl<double>(tx, ty) : stage_smem_impl<float>(tx, ty);
+    (void)ty;
+    const int nt = tx <= 58 ? 64 : 128;
+    return prec == HIS_PREC_F64 ? stage_smem_impl<double>(nt) : stage_smem_impl<float>(nt);
 }
 int engine_enqueue_f32(his_engine* e, int n) { return engine_enqueue_impl<float>(e, n); }
 int engine_take_rate_f32(his_engine* e) { return engine_take_rate_impl<float>(e); }

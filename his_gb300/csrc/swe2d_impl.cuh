@@ -1,75 +1,84 @@
-// Precision-templated host launchers of the 2-D kernels and the weir exchange.
-// Included once per precision by swe2d_f64.cu and swe2d_f32.cu.
+// Precision-templated host launchers of the 2-D strip kernels, the weir exchange and
+// the device-resident engine.  Included once per precision by swe2d_f64.cu and
+// swe2d_f32.cu.
 #pragma once
+#include <algorithm>
 #include <vector>
 
+#include "engine_kernels.cuh"
 #include "his_internal.h"
 #include "net1d_kernels.cuh"
-#include "swe2d_kernels.cuh"
-#include "engine_kernels.cuh"
+#include "swe2d_strip.cuh"
 
 namespace his {
 
-template <class R, int TX, int TY>
-int set_tile_attrs() {
-    using G = TileGeom<R, TX, TY>;
-    const int bytes = (int)G::smem_bytes;
-    HIS_CK(cudaFuncSetAttribute(stage_kernel<R, TX, TY, 0>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes));
-    HIS_CK(cudaFuncSetAttribute(stage_kernel<R, TX, TY, 1>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes));
-    HIS_CK(cudaFuncSetAttribute(stage_kernel<R, TX, TY, 2>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes));
+template <class R, int NT>
+int set_strip_attrs() {
+    const int bytes = (int)StripGeom<R, NT>::smem_bytes;
+    HIS_CK(cudaFuncSetAttribute(strip_kernel<R, NT, 0>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes));
+    HIS_CK(cudaFuncSetAttribute(strip_kernel<R, NT, 1>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes));
+    HIS_CK(cudaFuncSetAttribute(strip_kernel<R, NT, 2>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes));
     return HIS_OK;
 }
 
-template <class R, int TX, int TY>
-int launch_step_shape(his_grid* g, cudaStream_t s) {
-    using G = TileGeom<R, TX, TY>;
+// The 2-D stages of one step on stream s (no finalize).
+template <class R, int NT>
+int launch_stages(his_grid* g, cudaStream_t s) {
+    using G = StripGeom<R, NT>;
     auto* grids = reinterpret_cast<const Grid<R>*>(g->d_grids);
+    const KC<R> kc = make_kc<R>(g->c);
+    auto* strips = reinterpret_cast<const StripRef*>(g->d_tiles);
     if (g->c.order == 2) {
-        stage_kernel<R, TX, TY, 1><<<g->n_tiles, G::NT, G::smem_bytes, s>>>(grids, g->d_tiles, g->d_params,
-                                                                            make_kc<R>(g->c), g->d_partials);
-        stage_kernel<R, TX, TY, 2><<<g->n_tiles, G::NT, G::smem_bytes, s>>>(grids, g->d_tiles, g->d_params,
-                                                                            make_kc<R>(g->c), g->d_partials);
+        strip_kernel<R, NT, 1><<<g->n_tiles, NT, G::smem_bytes, s>>>(grids, strips, g->d_params, kc, g->d_partials);
+        strip_kernel<R, NT, 2><<<g->n_tiles, NT, G::smem_bytes, s>>>(grids, strips, g->d_params, kc, g->d_partials);
     } else {
-        stage_kernel<R, TX, TY, 0><<<g->n_tiles, G::NT, G::smem_bytes, s>>>(grids, g->d_tiles, g->d_params,
-                                                                            make_kc<R>(g->c), g->d_partials);
+        strip_kernel<R, NT, 0><<<g->n_tiles, NT, G::smem_bytes, s>>>(grids, strips, g->d_params, kc, g->d_partials);
+        stage_copy_kernel<R, NT><<<g->n_tiles, NT, 0, s>>>(grids, strips, g->d_params);
     }
-    finalize_kernel<R><<<g->n, 32, 0, s>>>(grids, g->d_params, g->c, g->d_partials, g->d_out, 0);
     HIS_CK(cudaGetLastError());
     return HIS_OK;
 }
 
-template <class R, int TX, int TY>
-int launch_reduce_shape(his_grid* g, cudaStream_t s) {
+template <class R, int NT>
+int launch_step_nt(his_grid* g, cudaStream_t s) {
+    int rc = launch_stages<R, NT>(g, s);
+    if (rc) return rc;
+    finalize_kernel<R><<<g->n, 32, 0, s>>>(reinterpret_cast<const Grid<R>*>(g->d_grids), g->d_params, g->c,
+                                           g->d_partials, g->d_out, 0);
+    HIS_CK(cudaGetLastError());
+    return HIS_OK;
+}
+
+template <class R, int NT>
+int launch_reduce_nt(his_grid* g, cudaStream_t s) {
     auto* grids = reinterpret_cast<const Grid<R>*>(g->d_grids);
-    cell_reduce_kernel<R, TX, TY><<<g->n_tiles, TX * TY, 0, s>>>(grids, g->d_tiles, make_kc<R>(g->c), g->d_partials);
+    strip_reduce_kernel<R, NT><<<g->n_tiles, NT, 0, s>>>(grids, reinterpret_cast<const StripRef*>(g->d_tiles),
+                                                         make_kc<R>(g->c), g->d_partials);
     finalize_kernel<R><<<g->n, 32, 0, s>>>(grids, g->d_params, g->c, g->d_partials, g->d_out, 1);
     HIS_CK(cudaGetLastError());
     return HIS_OK;
 }
 
-#define HIS_TILE_DISPATCH(FN, R, g, ...)                                      \
-    do {                                                                      \
-        if (g->tx == 32 && g->ty == 8) return FN<R, 32, 8>(g, __VA_ARGS__);   \
-        if (g->tx == 32 && g->ty == 16) return FN<R, 32, 16>(g, __VA_ARGS__); \
-        if (g->tx == 64 && g->ty == 4) return FN<R, 64, 4>(g, __VA_ARGS__);   \
-        if (g->tx == 16 && g->ty == 16) return FN<R, 16, 16>(g, __VA_ARGS__); \
-        set_error("unsupported tile shape");                                  \
-        return HIS_ERR_BAD_ARG;                                               \
+#define HIS_NT_DISPATCH(FN, R, g, ...)                           \
+    do {                                                         \
+        if (g->nt == 64) return FN<R, 64>(g, __VA_ARGS__);       \
+        if (g->nt == 128) return FN<R, 128>(g, __VA_ARGS__);     \
+        set_error("unsupported strip width (threads per CTA)");  \
+        return HIS_ERR_BAD_ARG;                                  \
     } while (0)
 
+// Strip decomposition of every member: columns in ceil(nx / (NT - 6)) strips of equal
+// width, rows in chunks of `ty` rows; the work units are listed member by member.
 template <class R>
 int grid_init_impl(his_grid* g) {
     int rc;
-    if ((rc = set_tile_attrs<R, 32, 8>()) != HIS_OK) return rc;
-    if ((rc = set_tile_attrs<R, 32, 16>()) != HIS_OK) return rc;
-    if ((rc = set_tile_attrs<R, 64, 4>()) != HIS_OK) return rc;
-    if ((rc = set_tile_attrs<R, 16, 16>()) != HIS_OK) return rc;
+    if ((rc = set_strip_attrs<R, 64>()) != HIS_OK) return rc;
+    if ((rc = set_strip_attrs<R, 128>()) != HIS_OK) return rc;
     const int n = g->n;
     std::vector<Grid<R>> H(n);
-    std::vector<TileRef> tiles;
+    std::vector<StripRef> strips;
     g->tile0.assign(n, 0);
     g->ntile.assign(n, 0);
-    // stage buffers: three planes per member, each 256-byte aligned
     std::vector<size_t> off(n);
     size_t total = 0;
     for (int m = 0; m < n; ++m) {
@@ -80,6 +89,7 @@ int grid_init_impl(his_grid* g) {
     }
     g->scratch_bytes = total;
     HIS_CK(cudaMalloc(&g->d_scratch, total > 0 ? total : 256));
+    const int wmax = g->tx;
     for (int m = 0; m < n; ++m) {
         const his_grid_desc& d = g->desc[m];
         Grid<R>& G = H[m];
@@ -93,15 +103,21 @@ int grid_init_impl(his_grid* g) {
         G.rdx = R(d.dx);
         G.rdy = R(d.dy);
         G.rt0 = R(d.horton_t0);
-        G.tiles_x = (d.nx + g->tx - 1) / g->tx;
-        G.tiles_y = (d.ny + g->ty - 1) / g->ty;
-        G.n_tiles = G.tiles_x * G.tiles_y;
-        G.tile0 = (int)tiles.size();
+        const int ns = (d.nx + wmax - 1) / wmax;
+        const int w = (d.nx + ns - 1) / ns;
+        const int nch = (d.ny + g->ty - 1) / g->ty;
+        const int hch = (d.ny + nch - 1) / nch;          // balanced chunk height <= ty
+        G.tiles_x = ns;
+        G.tiles_y = nch;
+        G.n_tiles = ns * nch;
+        G.tile0 = (int)strips.size();
         g->tile0[m] = G.tile0;
         g->ntile[m] = G.n_tiles;
-        for (int ty = 0; ty < G.tiles_y; ++ty)
-            for (int tx = 0; tx < G.tiles_x; ++tx)
-                tiles.push_back(TileRef{m, tx * g->tx, ty * g->ty, ty * G.tiles_x + tx});
+        for (int cy = 0; cy < nch; ++cy)
+            for (int sx = 0; sx < ns; ++sx) {
+                const int x0 = sx * w, y0 = cy * hch;
+                strips.push_back(StripRef{m, x0, std::min(w, d.nx - x0), y0, std::min(y0 + hch, d.ny), 0});
+            }
         G.h = (R*)d.h; G.hu = (R*)d.hu; G.hv = (R*)d.hv; G.sf = (R*)d.s_filled; G.ic = (R*)d.infil_cum;
         size_t plane = ((size_t)d.ny * d.nx * sizeof(R) + 255) & ~size_t(255);
         char* base = (char*)g->d_scratch + off[m];
@@ -110,25 +126,25 @@ int grid_init_impl(his_grid* g) {
         G.f0 = (const R*)d.f0; G.fc = (const R*)d.fc; G.k = (const R*)d.k; G.rw = (const R*)d.rain_weight;
         G.pk = (R*)d.peak_h; G.ps = (R*)d.peak_speed;
     }
-    g->n_tiles = (int)tiles.size();
+    g->n_tiles = (int)strips.size();
     HIS_CK(cudaMalloc(&g->d_grids, sizeof(Grid<R>) * n));
     HIS_CK(cudaMemcpy(g->d_grids, H.data(), sizeof(Grid<R>) * n, cudaMemcpyHostToDevice));
-    HIS_CK(cudaMalloc(&g->d_tiles, sizeof(TileRef) * tiles.size()));
-    HIS_CK(cudaMemcpy(g->d_tiles, tiles.data(), sizeof(TileRef) * tiles.size(), cudaMemcpyHostToDevice));
+    HIS_CK(cudaMalloc(&g->d_tiles, sizeof(StripRef) * strips.size()));
+    HIS_CK(cudaMemcpy(g->d_tiles, strips.data(), sizeof(StripRef) * strips.size(), cudaMemcpyHostToDevice));
     HIS_CK(cudaMalloc(&g->d_partials, sizeof(double) * NPART * (size_t)g->n_tiles));
     HIS_CK(cudaMemset(g->d_partials, 0, sizeof(double) * NPART * (size_t)g->n_tiles));
-    g->table_bytes = sizeof(Grid<R>) * n + sizeof(TileRef) * tiles.size() + sizeof(double) * NPART * g->n_tiles;
+    g->table_bytes = sizeof(Grid<R>) * n + sizeof(StripRef) * strips.size() + sizeof(double) * NPART * g->n_tiles;
     return HIS_OK;
 }
 
 template <class R>
 int grid_step_impl(his_grid* g, cudaStream_t s) {
-    HIS_TILE_DISPATCH(launch_step_shape, R, g, s);
+    HIS_NT_DISPATCH(launch_step_nt, R, g, s);
 }
 
 template <class R>
 int grid_reduce_impl(his_grid* g, cudaStream_t s) {
-    HIS_TILE_DISPATCH(launch_reduce_shape, R, g, s);
+    HIS_NT_DISPATCH(launch_reduce_nt, R, g, s);
 }
 
 template <class R>
@@ -143,21 +159,17 @@ int exchange_impl(his_links* l, const Consts& c, double dt, cudaStream_t s) {
 }
 
 template <class R>
-size_t stage_smem_impl(int tx, int ty) {
-    if (tx == 32 && ty == 8) return TileGeom<R, 32, 8>::smem_bytes;
-    if (tx == 32 && ty == 16) return TileGeom<R, 32, 16>::smem_bytes;
-    if (tx == 64 && ty == 4) return TileGeom<R, 64, 4>::smem_bytes;
-    if (tx == 16 && ty == 16) return TileGeom<R, 16, 16>::smem_bytes;
+size_t stage_smem_impl(int nt) {
+    if (nt == 64) return StripGeom<R, 64>::smem_bytes;
+    if (nt == 128) return StripGeom<R, 128>::smem_bytes;
     return 0;
 }
-
 
 // One device-resident step for every member (see engine_kernels.cuh); the 1-D
 // substeps run on the side stream between a fork and a join event, concurrently
 // with the 2-D stages.
-template <class R, int TX, int TY>
-int eng_enqueue_shape(his_grid* g, his_engine* E, int n_steps) {
-    using G = TileGeom<R, TX, TY>;
+template <class R, int NT>
+int eng_enqueue_nt(his_grid* g, his_engine* E, int n_steps) {
     auto* grids = reinterpret_cast<const Grid<R>*>(g->d_grids);
     const Net* nets = E->net ? E->net->d_nets : nullptr;
     const Lnk* links = E->links ? E->links->d_links : nullptr;
@@ -172,15 +184,8 @@ int eng_enqueue_shape(his_grid* g, his_engine* E, int n_steps) {
             if (rc) return rc;
             HIS_CK(cudaEventRecord(E->ev_join, E->s1));
         }
-        if (g->c.order == 2) {
-            stage_kernel<R, TX, TY, 1><<<g->n_tiles, G::NT, G::smem_bytes, E->s0>>>(grids, g->d_tiles, g->d_params,
-                                                                                    make_kc<R>(g->c), g->d_partials);
-            stage_kernel<R, TX, TY, 2><<<g->n_tiles, G::NT, G::smem_bytes, E->s0>>>(grids, g->d_tiles, g->d_params,
-                                                                                    make_kc<R>(g->c), g->d_partials);
-        } else {
-            stage_kernel<R, TX, TY, 0><<<g->n_tiles, G::NT, G::smem_bytes, E->s0>>>(grids, g->d_tiles, g->d_params,
-                                                                                    make_kc<R>(g->c), g->d_partials);
-        }
+        int rc = launch_stages<R, NT>(g, E->s0);
+        if (rc) return rc;
         if (E->net) HIS_CK(cudaStreamWaitEvent(E->s0, E->ev_join, 0));
         eng_post_kernel<R><<<E->n, 32, 0, E->s0>>>(E->d_em, g->d_params, grids, g->c, g->d_partials,
                                                    E->net ? E->d_vol1d : nullptr, g->d_out);
@@ -192,7 +197,7 @@ int eng_enqueue_shape(his_grid* g, his_engine* E, int n_steps) {
 template <class R>
 int engine_enqueue_impl(his_engine* E, int n_steps) {
     his_grid* g = E->grid;
-    HIS_TILE_DISPATCH(eng_enqueue_shape, R, g, E, n_steps);
+    HIS_NT_DISPATCH(eng_enqueue_nt, R, g, E, n_steps);
 }
 
 template <class R>
@@ -207,15 +212,17 @@ int engine_take_rate_impl(his_engine* E) {
     return HIS_OK;
 }
 
-// Same step sequence as eng_enqueue_shape, uncaptured, with CUDA events around each
+// Same step sequence as eng_enqueue_nt, uncaptured, with CUDA events around each
 // kernel class on its own stream; accumulates device milliseconds into ms[6].
-template <class R, int TX, int TY>
-int eng_profile_shape(his_grid* g, his_engine* E, int n_steps, double* ms) {
-    using G = TileGeom<R, TX, TY>;
+template <class R, int NT>
+int eng_profile_nt(his_grid* g, his_engine* E, int n_steps, double* ms) {
+    using G = StripGeom<R, NT>;
     auto* grids = reinterpret_cast<const Grid<R>*>(g->d_grids);
     const Net* nets = E->net ? E->net->d_nets : nullptr;
     const Lnk* links = E->links ? E->links->d_links : nullptr;
     double* exch = E->links ? E->links->d_exch : nullptr;
+    const KC<R> kc = make_kc<R>(g->c);
+    auto* strips = reinterpret_cast<const StripRef*>(g->d_tiles);
     cudaEvent_t ev[7];
     for (auto& e : ev) HIS_CK(cudaEventCreate(&e));
     int rc = HIS_OK;
@@ -231,15 +238,16 @@ int eng_profile_shape(his_grid* g, his_engine* E, int n_steps, double* ms) {
             cudaEventRecord(ev[5], E->s1);
         }
         if (g->c.order == 2) {
-            stage_kernel<R, TX, TY, 1><<<g->n_tiles, G::NT, G::smem_bytes, E->s0>>>(grids, g->d_tiles, g->d_params,
-                                                                                    make_kc<R>(g->c), g->d_partials);
+            strip_kernel<R, NT, 1><<<g->n_tiles, NT, G::smem_bytes, E->s0>>>(grids, strips, g->d_params, kc,
+                                                                            g->d_partials);
             cudaEventRecord(ev[2], E->s0);
-            stage_kernel<R, TX, TY, 2><<<g->n_tiles, G::NT, G::smem_bytes, E->s0>>>(grids, g->d_tiles, g->d_params,
-                                                                                    make_kc<R>(g->c), g->d_partials);
+            strip_kernel<R, NT, 2><<<g->n_tiles, NT, G::smem_bytes, E->s0>>>(grids, strips, g->d_params, kc,
+                                                                            g->d_partials);
         } else {
             cudaEventRecord(ev[2], E->s0);
-            stage_kernel<R, TX, TY, 0><<<g->n_tiles, G::NT, G::smem_bytes, E->s0>>>(grids, g->d_tiles, g->d_params,
-                                                                                    make_kc<R>(g->c), g->d_partials);
+            strip_kernel<R, NT, 0><<<g->n_tiles, NT, G::smem_bytes, E->s0>>>(grids, strips, g->d_params, kc,
+                                                                            g->d_partials);
+            stage_copy_kernel<R, NT><<<g->n_tiles, NT, 0, E->s0>>>(grids, strips, g->d_params);
         }
         cudaEventRecord(ev[3], E->s0);
         if (E->net) cudaStreamWaitEvent(E->s0, ev[5], 0);
@@ -264,7 +272,7 @@ int eng_profile_shape(his_grid* g, his_engine* E, int n_steps, double* ms) {
 template <class R>
 int engine_profile_impl(his_engine* E, int n_steps, double* ms) {
     his_grid* g = E->grid;
-    HIS_TILE_DISPATCH(eng_profile_shape, R, g, E, n_steps, ms);
+    HIS_NT_DISPATCH(eng_profile_nt, R, g, E, n_steps, ms);
 }
 
 }  // namespace his

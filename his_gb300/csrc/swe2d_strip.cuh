@@ -1,0 +1,600 @@
+// 2-D finite-volume step kernels: row-marching strips.
+//
+// A CTA of NT threads owns a strip of W <= NT - 6 columns of one member and marches
+// up a chunk of rows [y0, y1).  Thread t works on column cx = x0 - 3 + t.  Per new
+// row r it
+//   P1  loads row r of (h, u, v, z) into a ring of 8 rows (ghost cells built at the
+//       domain edges, boundaries.py:81-128),
+//   P2  computes the y-face between rows r-2 and r-1 (the lower cell's
+//       y-reconstruction is carried in registers from the previous row) and the
+//       x-reconstruction of row r-2,
+//   P3  computes the x-faces of row r-2,
+//   P4  computes the positivity-limiter theta of row r-2 (swe2d.py:259-264),
+//   P5  updates row r-3 (divergence of the donor-scaled fluxes, bed source, RK
+//       stage, then in the last stage rain, infiltration, retention, friction, CFL
+//       rate and peaks; swe2d.py:305-371).
+// Every cell is loaded once (plus a 3-column halo each side) and every face flux,
+// reconstruction and theta is computed once.  Per-thread partial sums (clip,
+// boundary flux, infiltration, rain, rate, volumes) are reduced once per strip-chunk
+// into one float64 slot set, summed in a fixed order per member by the finalize
+// kernel, so results do not depend on the batch a member runs in.
+#pragma once
+#include "his_device.cuh"
+
+namespace his {
+
+struct StripRef {
+    int member, x0, w, y0, y1, pad;
+};
+
+// Shared-memory layout of one CTA
+template <class R, int NT>
+struct StripGeom {
+    static constexpr int RING = 8;                 // cell rows kept
+    static constexpr int FR = 4;                   // face / theta rows kept
+    static constexpr int NREC = 10;                // x-reconstruction values per cell
+    static constexpr int NRED = 11;
+    static constexpr size_t cells = (size_t)RING * NT * 4;
+    static constexpr size_t xrec = (size_t)NREC * NT;
+    static constexpr size_t xf = (size_t)FR * NT * 4;
+    static constexpr size_t yf = (size_t)FR * NT * 4;
+    static constexpr size_t th = (size_t)FR * NT;
+    static constexpr size_t smem_bytes = sizeof(R) * (cells + xrec + xf + yf + th) + sizeof(R) * 32 * NRED + 32;
+};
+
+// Bed source of one cell along one axis (swe2d.py:220); float32: the bed source plus
+// the hydrostatic part of the face momentum fluxes, -g/2 (H+ + H-) sE (see riemann_wb).
+template <class R>
+__device__ __forceinline__ R bed_source(const KC<R>& c, R hm, R h0, R hp, R zm, R z0, R zp) {
+    R hmin = rmin(rmin(hm, h0), hp);
+    R ok = (hmin >= c.h_dry) ? R(1) : R(0);
+    R sH = minmod(h0 - hm, hp - h0) * ok;
+    R Hm = h0 - R(0.5) * sH, Hp = h0 + R(0.5) * sH;
+    if constexpr (sizeof(R) == 8) {
+        R em = hm + zm, e0 = h0 + z0, ep = hp + zp;
+        R sE = minmod(e0 - em, ep - e0) * ok;
+        R Em = e0 - R(0.5) * sE, Ep = e0 + R(0.5) * sE;
+        R Zm = Em - Hm, Zp = Ep - Hp;
+        return c.nhg * (Hm + Hp) * (Zp - Zm);
+    } else {
+        R sE = minmod((h0 - hm) + (z0 - zm), (hp - h0) + (zp - z0)) * ok;
+        return c.nhg * (Hm + Hp) * sE;
+    }
+}
+
+// One halo position: an interior cell, or the ghost that the x-sweep (outside in x)
+// or the y-sweep (outside in y) would see (boundaries.py:81-128), in two parts for
+// software pipelining: halo_fetch issues the loads of the source cell (the cell
+// itself, or the layer a ghost copies) rows ahead; halo_build turns the fetched raw
+// values into (h, u, v, z) when the row is due.
+template <class R>
+struct HaloRaw {
+    R h, hu, hv, z;
+};
+
+template <class R>
+__device__ __forceinline__ HaloRaw<R> halo_fetch(const KC<R>& c, const Grid<R>& gd, const R* __restrict__ H,
+                                                 const R* __restrict__ HU, const R* __restrict__ HV, int gx, int gy) {
+    const int nx = gd.nx, ny = gd.ny;
+    const bool inx = (unsigned)gx < (unsigned)nx, iny = (unsigned)gy < (unsigned)ny;
+    HaloRaw<R> a;
+    if (!inx && !iny) { a.h = a.hu = a.hv = a.z = R(0); return a; }
+    size_t i;
+    if (inx && iny) {
+        i = (size_t)gy * nx + gx;
+    } else {
+        const int ng = c.order == 1 ? 1 : 2;
+        const bool alongx = !inx;
+        const int n = alongx ? nx : ny;
+        const int gpos = alongx ? gx : gy;
+        const bool lo = gpos < 0;
+        const int side = alongx ? (lo ? EDGE_W : EDGE_E) : (lo ? EDGE_S : EDGE_N);
+        const int k = lo ? (-gpos - 1) : (gpos - n);
+        const int kind = gd.bc[side];
+        int layer;
+        if (kind == BC_CLOSED || kind == BC_TRANSMISSIVE) {
+            if (n < ng) layer = lo ? 0 : n - 1;
+            else layer = lo ? k : n - 1 - k;
+        } else {
+            layer = lo ? 0 : n - 1;
+        }
+        layer = layer < 0 ? 0 : (layer > n - 1 ? n - 1 : layer);
+        i = alongx ? (size_t)gy * nx + layer : (size_t)layer * nx + gx;
+    }
+    a.h = H[i];
+    a.hu = HU[i];
+    a.hv = HV[i];
+    a.z = gd.z[i];
+    return a;
+}
+
+template <class R>
+__device__ __forceinline__ void halo_build(const KC<R>& c, const Grid<R>& gd, const R* bcv, const HaloRaw<R>& a,
+                                           int gx, int gy, R& hh, R& uu, R& vv, R& zz) {
+    const int nx = gd.nx, ny = gd.ny;
+    const bool inx = (unsigned)gx < (unsigned)nx, iny = (unsigned)gy < (unsigned)ny;
+    if (!inx && !iny) { hh = uu = vv = zz = R(0); return; }
+    R u0, v0;
+    kp_velocity(c, a.h, a.hu, a.hv, u0, v0);
+    zz = a.z;
+    if (inx && iny) { hh = a.h; uu = u0; vv = v0; return; }
+    const bool alongx = !inx;
+    const int n = alongx ? nx : ny;
+    const int gpos = alongx ? gx : gy;
+    const bool lo = gpos < 0;
+    const int side = alongx ? (lo ? EDGE_W : EDGE_E) : (lo ? EDGE_S : EDGE_N);
+    const int kind = gd.bc[side];
+    (void)n;
+    const R sgn = lo ? R(-1) : R(1);
+    R un = sgn * (alongx ? u0 : v0);
+    R ut = alongx ? v0 : u0;
+    R hg, ung, utg;
+    if (kind == BC_CLOSED) { hg = a.h; ung = -un; utg = ut; }
+    else if (kind == BC_TRANSMISSIVE) { hg = a.h; ung = un; utg = ut; }
+    else if (kind == BC_STAGE) stage_ghost(c, bcv[side], a.h, un, ut, a.z, hg, ung, utg);
+    else discharge_ghost(c, bcv[side], a.h, hg, ung, utg);
+    hh = hg;
+    if (alongx) { uu = sgn * ung; vv = utg; }
+    else { vv = sgn * ung; uu = utg; }
+}
+
+// Per-cell inputs of the update (row orow), fetched one row ahead.
+template <class R>
+struct CellIn {
+    R h0, hu0, hv0, hu1, hv1, sf, ic, f0, fc, k, S, n, rw;
+};
+
+template <class R, int STAGE>
+__device__ __forceinline__ CellIn<R> cell_fetch(const Grid<R>& gd, size_t i) {
+    CellIn<R> a;
+    a.hu0 = gd.hu[i];
+    a.hv0 = gd.hv[i];
+    if (STAGE == 2) {
+        a.h0 = gd.h[i];
+        a.hu1 = gd.hu1[i];
+        a.hv1 = gd.hv1[i];
+    } else {
+        a.h0 = a.hu1 = a.hv1 = R(0);
+    }
+    if (STAGE != 1) {
+        a.sf = gd.S ? gd.sf[i] : R(0);
+        a.S = gd.S ? gd.S[i] : R(0);
+        a.ic = gd.f0 ? gd.ic[i] : R(0);
+        a.f0 = gd.f0 ? gd.f0[i] : R(0);
+        a.fc = gd.f0 ? gd.fc[i] : R(0);
+        a.k = gd.f0 ? gd.k[i] : R(0);
+        a.n = gd.n[i];
+        a.rw = gd.rw ? gd.rw[i] : R(0);
+    } else {
+        a.sf = a.S = a.ic = a.f0 = a.fc = a.k = a.n = a.rw = R(0);
+    }
+    return a;
+}
+
+template <class T>
+__device__ __forceinline__ T warp_sum_t(T v) {
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+    return v;
+}
+template <class T>
+__device__ __forceinline__ T warp_max_t(T v) {
+    for (int o = 16; o > 0; o >>= 1) {
+        T w = __shfl_down_sync(0xffffffffu, v, o);
+        v = w > v ? w : v;
+    }
+    return v;
+}
+
+// Block reduction of NV per-thread values in the compute type T (warps by shuffles,
+// then lane j of warp 0 over the warps in order), one float64 store per value.
+template <int NV, class T>
+__device__ __forceinline__ void block_reduce_store(T (&v)[NV], const bool* is_max, T* red, double* out,
+                                                   const int* slots, int nthreads) {
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = nthreads >> 5;
+#pragma unroll
+    for (int j = 0; j < NV; ++j) v[j] = is_max[j] ? warp_max_t(v[j]) : warp_sum_t(v[j]);
+    if (lane == 0) {
+#pragma unroll
+        for (int j = 0; j < NV; ++j) red[warp * NV + j] = v[j];
+    }
+    __syncthreads();
+    if (warp == 0 && lane < NV) {
+        const bool mx = is_max[lane];
+        T a = red[lane];
+        for (int w = 1; w < nw; ++w) {
+            const T b = red[w * NV + lane];
+            a = mx ? (b > a ? b : a) : a + b;
+        }
+        out[slots[lane]] = (double)a;
+    }
+}
+
+template <class R>
+__device__ __forceinline__ void store_recon(R* xr, int stride, int t, const Recon<R>& r) {
+    xr[0 * stride + t] = r.Hm; xr[1 * stride + t] = r.Hp;
+    xr[2 * stride + t] = r.Um; xr[3 * stride + t] = r.Up;
+    xr[4 * stride + t] = r.Vm; xr[5 * stride + t] = r.Vp;
+    if constexpr (sizeof(R) == 8) {
+        xr[6 * stride + t] = r.Zm; xr[7 * stride + t] = r.Zp;
+    } else {
+        xr[6 * stride + t] = r.z; xr[7 * stride + t] = r.d;
+        xr[8 * stride + t] = r.h0; xr[9 * stride + t] = r.sE;
+    }
+}
+
+template <class R>
+__device__ __forceinline__ Recon<R> load_recon(const R* xr, int stride, int t) {
+    Recon<R> r;
+    r.Hm = xr[0 * stride + t]; r.Hp = xr[1 * stride + t];
+    r.Um = xr[2 * stride + t]; r.Up = xr[3 * stride + t];
+    r.Vm = xr[4 * stride + t]; r.Vp = xr[5 * stride + t];
+    if constexpr (sizeof(R) == 8) {
+        r.Zm = xr[6 * stride + t]; r.Zp = xr[7 * stride + t];
+        r.z = r.d = r.h0 = r.sE = R(0);
+    } else {
+        r.z = xr[6 * stride + t]; r.d = xr[7 * stride + t];
+        r.h0 = xr[8 * stride + t]; r.sE = xr[9 * stride + t];
+        r.Zm = r.Zp = R(0);
+    }
+    return r;
+}
+
+// STAGE: 0 = first-order full step, 1 = RK stage 1, 2 = RK stage 2 + sources.
+// Stage 1 writes the stage buffers; stage 2 reads them in its halo and writes the
+// state.  The first-order step reads the state in its halo, so it writes its result
+// to the stage buffers and stage_copy_kernel moves it back (no CTA overwrites cells
+// that another CTA may still read).
+template <class R, int NT, int STAGE>
+__global__ void __launch_bounds__(NT) strip_kernel(const Grid<R>* __restrict__ grids,
+                                                    const StripRef* __restrict__ strips,
+                                                    const StepParams* __restrict__ params, const KC<R> c,
+                                                    double* __restrict__ partials) {
+    using G = StripGeom<R, NT>;
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    R* s_h = reinterpret_cast<R*>(smem_raw);          // [RING][NT]
+    R* s_u = s_h + G::RING * NT;
+    R* s_v = s_u + G::RING * NT;
+    R* s_z = s_v + G::RING * NT;
+    R* s_xr = s_z + G::RING * NT;                     // [NREC][NT]
+    R* s_xf1 = s_xr + G::NREC * NT;                   // [FR][NT] each
+    R* s_xf2l = s_xf1 + G::FR * NT;
+    R* s_xf2r = s_xf2l + G::FR * NT;
+    R* s_xf3 = s_xf2r + G::FR * NT;
+    R* s_yf1 = s_xf3 + G::FR * NT;
+    R* s_yf2l = s_yf1 + G::FR * NT;
+    R* s_yf2r = s_yf2l + G::FR * NT;
+    R* s_yf3 = s_yf2r + G::FR * NT;
+    R* s_th = s_yf3 + G::FR * NT;                     // [FR][NT]
+    R* red = reinterpret_cast<R*>((reinterpret_cast<uintptr_t>(s_th + G::FR * NT) + 15) & ~uintptr_t(15));
+    __shared__ R bcv[4];
+
+    const StripRef sr = strips[blockIdx.x];
+    const Grid<R>& gd = grids[sr.member];
+    const StepParams& pr = params[sr.member];
+    if (!pr.active) return;
+    const int t = threadIdx.x;
+    const int nx = gd.nx, ny = gd.ny;
+    const int x0 = sr.x0, W = sr.w, y0 = sr.y0, y1 = sr.y1;
+    const int cx = x0 - 3 + t;                        // this thread's column
+    const R dt = par_dt<R>(pr);
+    if (t < 4) bcv[t] = par_bc<R>(pr, STAGE == 2, t);
+    const R* __restrict__ H = STAGE == 2 ? gd.h1 : gd.h;
+    const R* __restrict__ HU = STAGE == 2 ? gd.hu1 : gd.hu;
+    const R* __restrict__ HV = STAGE == 2 ? gd.hv1 : gd.hv;
+    const R rdx = gd.rdx, rdy = gd.rdy;
+    const R rdt = par_rain<R>(pr) * dt;
+    const R tt = clamp0(par_t<R>(pr) - gd.rt0);
+    const bool col_in = (unsigned)cx < (unsigned)nx;
+    const int q = cx - x0;                                      // column relative to the strip
+    const bool do_yface = q >= -1 && q <= W && col_in;
+    const bool do_xrec = q >= -2 && q <= W + 1;
+    const bool do_xface = q >= -1 && q <= W + 1 && cx >= 0 && cx <= nx;
+    const bool do_theta = q >= -1 && q <= W;                    // theta = 1 outside the domain
+    const bool do_out = q >= 0 && q < W && col_in;
+
+    R acc_clip = 0, xin = 0, xout = 0, yin = 0, yout = 0, infil = 0, rainw = 0, rate = 0, hsum = 0, ssum = 0;
+    R hmax = 0;
+    Recon<R> ylow;                                   // y-reconstruction of row r-2 (carried)
+    // software pipeline: halo rows are fetched two rows ahead, update inputs one row ahead
+    HaloRaw<R> ra = halo_fetch(c, gd, H, HU, HV, cx, y0 - 3);
+    HaloRaw<R> rb = halo_fetch(c, gd, H, HU, HV, cx, y0 - 2);
+    CellIn<R> cin;
+    __syncthreads();
+
+    for (int r = y0 - 3; r <= y1 + 2; ++r) {
+        // ---- P1: build row r from values fetched two rows ago; fetch row r + 2 and the
+        //      update inputs of row r - 2
+        const int sl = r & (G::RING - 1);
+        const HaloRaw<R> rnext = halo_fetch(c, gd, H, HU, HV, cx, r + 2);
+        const int nrow = r - 2;
+        const bool fetch_in = do_out && nrow >= y0 && nrow < y1;
+        CellIn<R> cnext;
+        if (fetch_in) cnext = cell_fetch<R, STAGE>(gd, (size_t)nrow * nx + cx);
+        {
+            R hh, uu, vv, zz;
+            halo_build(c, gd, bcv, ra, cx, r, hh, uu, vv, zz);
+            s_h[sl * NT + t] = hh; s_u[sl * NT + t] = uu; s_v[sl * NT + t] = vv; s_z[sl * NT + t] = zz;
+        }
+        ra = rb;
+        rb = rnext;
+        __syncthreads();
+        // ---- P2: y-face between rows r-2 and r-1 (face index r-1), x-reconstruction of row r-2
+        if (r >= y0 - 1) {
+            const int a = (r - 2) & (G::RING - 1), b = (r - 1) & (G::RING - 1), cslot = r & (G::RING - 1);
+            if (do_yface) {
+                // y-reconstruction of row r-1: normal v, tangential u
+                Recon<R> yup = reconstruct(c, s_h[a * NT + t], s_h[b * NT + t], s_h[cslot * NT + t],
+                                           s_v[a * NT + t], s_v[b * NT + t], s_v[cslot * NT + t],
+                                           s_u[a * NT + t], s_u[b * NT + t], s_u[cslot * NT + t],
+                                           s_z[a * NT + t], s_z[b * NT + t], s_z[cslot * NT + t]);
+                const int fy = r - 1;
+                if (r >= y0 && fy >= y0 - 1 && fy <= y1 + 1) {
+                    R F1 = R(0), F2L = R(0), F2R = R(0), F3 = R(0);
+                    if (fy >= 0 && fy <= ny) face_flux(c, ylow, yup, F1, F2L, F2R, F3);
+                    const int fs = (fy & (G::FR - 1)) * NT + t;
+                    s_yf1[fs] = F1; s_yf2l[fs] = F2L; s_yf2r[fs] = F2R; s_yf3[fs] = F3;
+                }
+                ylow = yup;
+            }
+            if (r >= y0 + 1 && do_xrec) {
+                const int rr = ((r - 2) & (G::RING - 1)) * NT;
+                Recon<R> xr = reconstruct(c, s_h[rr + t - 1], s_h[rr + t], s_h[rr + t + 1], s_u[rr + t - 1],
+                                          s_u[rr + t], s_u[rr + t + 1], s_v[rr + t - 1], s_v[rr + t],
+                                          s_v[rr + t + 1], s_z[rr + t - 1], s_z[rr + t], s_z[rr + t + 1]);
+                store_recon(s_xr, NT, t, xr);
+            }
+        }
+        __syncthreads();
+        if (r >= y0 + 1) {
+            const int row = r - 2;
+            // ---- P3: x-faces of row r-2 (face cx between columns cx-1 and cx)
+            if (do_xface && (unsigned)row < (unsigned)ny) {
+                Recon<R> L = load_recon(s_xr, NT, t - 1), Rr = load_recon(s_xr, NT, t);
+                R F1, F2L, F2R, F3;
+                face_flux(c, L, Rr, F1, F2L, F2R, F3);
+                const int fs = (row & (G::FR - 1)) * NT + t;
+                s_xf1[fs] = F1; s_xf2l[fs] = F2L; s_xf2r[fs] = F2R; s_xf3[fs] = F3;
+            }
+            __syncthreads();
+            // ---- P4: theta of row r-2
+            if (do_theta) {
+                R th = R(1);
+                if ((unsigned)row < (unsigned)ny && col_in) {
+                    const int fr = (row & (G::FR - 1)) * NT;
+                    const R Fw = s_xf1[fr + t], Fe = s_xf1[fr + t + 1];
+                    const R Gs = s_yf1[fr + t], Gn = s_yf1[((row + 1) & (G::FR - 1)) * NT + t];
+                    const R out = (relu(Fe) + relu(-Fw)) / rdx + (relu(Gn) + relu(-Gs)) / rdy;
+                    const R need = out * dt;
+                    const R hh = s_h[(row & (G::RING - 1)) * NT + t];
+                    th = need > hh ? hh / (need > R(0) ? need : R(1)) : R(1);
+                }
+                s_th[(row & (G::FR - 1)) * NT + t] = th;
+            }
+            __syncthreads();
+        }
+        // ---- P5: update row r-3
+        const int orow = r - 3;
+        if (orow >= y0 && orow < y1 && do_out) {
+            const int f0 = (orow & (G::FR - 1)) * NT, f1 = ((orow + 1) & (G::FR - 1)) * NT;
+            const int tc = f0 + t;
+            const R thC = s_th[tc], thW = s_th[tc - 1], thE = s_th[tc + 1];
+            const R thS = s_th[((orow - 1) & (G::FR - 1)) * NT + t], thN = s_th[f1 + t];
+            const R Fw = s_xf1[f0 + t], Fe = s_xf1[f0 + t + 1], Gs = s_yf1[f0 + t], Gn = s_yf1[f1 + t];
+            const R sw = Fw > R(0) ? thW : thC, se = Fe > R(0) ? thC : thE;
+            const R ss = Gs > R(0) ? thS : thC, sn = Gn > R(0) ? thC : thN;
+            const R F1w = Fw * sw, F1e = Fe * se, G1s = Gs * ss, G1n = Gn * sn;
+            R a1 = -(F1e - F1w) / rdx;
+            R a2 = -(s_xf2l[f0 + t + 1] - s_xf2r[f0 + t]) / rdx;
+            R a3 = -(s_xf3[f0 + t + 1] * se - s_xf3[f0 + t] * sw) / rdx;
+            R b1 = -(G1n - G1s) / rdy;
+            R b2 = -(s_yf2l[f1 + t] - s_yf2r[f0 + t]) / rdy;
+            R b3 = -(s_yf3[f1 + t] * sn - s_yf3[f0 + t] * ss) / rdy;
+            const int cm = ((orow - 1) & (G::RING - 1)) * NT + t, c0 = (orow & (G::RING - 1)) * NT + t;
+            const int cp = ((orow + 1) & (G::RING - 1)) * NT + t;
+            if (c.order == 2) {
+                R scx = bed_source(c, s_h[c0 - 1], s_h[c0], s_h[c0 + 1], s_z[c0 - 1], s_z[c0], s_z[c0 + 1]);
+                R scy = bed_source(c, s_h[cm], s_h[c0], s_h[cp], s_z[cm], s_z[c0], s_z[cp]);
+                a2 = a2 + scx / rdx;
+                b2 = b2 + scy / rdy;
+            }
+            const R dh = a1 + b1, dhu = a2 + b3, dhv = a3 + b2;
+            if (cx == 0) { xin += relu(F1w); xout += relu(-F1w); }
+            if (cx == nx - 1) { xin += relu(-F1e); xout += relu(F1e); }
+            if (orow == 0) { yin += relu(G1s); yout += relu(-G1s); }
+            if (orow == ny - 1) { yin += relu(-G1n); yout += relu(G1n); }
+            const size_t i = (size_t)orow * nx + cx;
+            R hn, hun, hvn;
+            if (STAGE == 2) {
+                const R h1 = s_h[c0];
+                hn = R(0.5) * (cin.h0 + h1 + dt * dh);
+                hun = R(0.5) * (cin.hu0 + cin.hu1 + dt * dhu);
+                hvn = R(0.5) * (cin.hv0 + cin.hv1 + dt * dhv);
+            } else {
+                hn = s_h[c0] + dt * dh;
+                hun = cin.hu0 + dt * dhu;
+                hvn = cin.hv0 + dt * dhv;
+            }
+            const R neg = clamp0(-hn);
+            acc_clip += neg;
+            hn = hn + neg;
+            if (STAGE == 1) {
+                gd.h1[i] = hn; gd.hu1[i] = hun; gd.hv1[i] = hvn;
+            } else {
+                // ---- rain, Horton infiltration, retention store (swe2d.py:330-360)
+                R sf = cin.sf;
+                if (gd.rw) {
+                    const R add = rdt * cin.rw;
+                    hn = hn + add;
+                    rainw += add;
+                } else {
+                    hn = hn + rdt;
+                }
+                if (gd.f0) {
+                    const R rate_f = cin.fc + (cin.f0 - cin.fc) * rexp(-cin.k * tt);
+                    const R pot = rate_f * dt;
+                    const R take = rmin(pot, hn);
+                    const R safe = hn > R(0) ? hn : R(1);
+                    const R scale = hn > R(0) ? (hn - take) / safe : R(0);
+                    hn = hn - take;
+                    hun = hun * scale;
+                    hvn = hvn * scale;
+                    R taken = take;
+                    if (gd.S) {
+                        const R tks = rmin(pot - take, sf);
+                        sf = sf - tks;
+                        taken = taken + tks;
+                    }
+                    infil += taken;
+                    gd.ic[i] = cin.ic + taken;
+                }
+                if (gd.S) {
+                    const R room = clamp0(cin.S - sf);
+                    const R fill = rmin(room, hn);
+                    const R safe = hn > R(0) ? hn : R(1);
+                    const R scale = hn > R(0) ? (hn - fill) / safe : R(0);
+                    hn = hn - fill;
+                    hun = hun * scale;
+                    hvn = hvn * scale;
+                    sf = sf + fill;
+                    gd.sf[i] = sf;
+                }
+                // ---- semi-implicit Manning friction (swe2d.py:362-370)
+                R u, v;
+                kp_velocity(c, hn, hun, hvn, u, v);
+                const R speed = dsqrt(u * u + v * v);
+                const R hf = rmax(hn, c.h_dry);
+                const R nm = cin.n;
+                const R denom = R(1) + dt * c.g * nm * nm * speed / pow43(hf);
+                u = u / denom;
+                v = v / denom;
+                const bool wet = hn >= c.h_dry;
+                hun = wet ? hn * u : R(0);
+                hvn = wet ? hn * v : R(0);
+                if (STAGE == 2) {
+                    gd.h[i] = hn; gd.hu[i] = hun; gd.hv[i] = hvn;
+                } else {
+                    gd.h1[i] = hn; gd.hu1[i] = hun; gd.hv1[i] = hvn;
+                }
+                if (gd.pk) gd.pk[i] = rmax(gd.pk[i], hn);
+                if (gd.ps) gd.ps[i] = rmax(gd.ps[i], wet ? dsqrt(u * u + v * v) : R(0));
+                // ---- CFL rate of the new state for the next step (swe2d.py:179-184)
+                R u2, v2;
+                kp_velocity(c, hn, hun, hvn, u2, v2);
+                const R cw = dsqrt(c.g * hn);
+                const R rr = hn > c.h_dry ? (fabs(u2) + cw) / rdx + (fabs(v2) + cw) / rdy : R(0);
+                rate = rmax(rate, rr);
+                hsum += hn;
+                ssum += sf;
+                hmax = rmax(hmax, hn);
+            }
+        }
+        if (fetch_in) cin = cnext;
+    }
+    __syncthreads();
+    double* out = partials + (size_t)blockIdx.x * NPART;
+    if (STAGE == 1) {
+        R v[5] = {acc_clip, xin, xout, yin, yout};
+        const bool mx[5] = {false, false, false, false, false};
+        const int sl[5] = {P_CLIP1, P_XIN1, P_XOUT1, P_YIN1, P_YOUT1};
+        block_reduce_store<5>(v, mx, red, out, sl, NT);
+    } else {
+        const int b = STAGE == 2 ? P_CLIP2 : P_CLIP1;
+        R v[11] = {acc_clip, xin, xout, yin, yout, infil, rainw, rate, hsum, ssum, hmax};
+        const bool mx[11] = {false, false, false, false, false, false, false, true, false, false, true};
+        const int sl[11] = {b, b + 1, b + 2, b + 3, b + 4, P_INFIL, P_RAINW, P_RATE, P_HSUM, P_SSUM, P_HMAX};
+        block_reduce_store<11>(v, mx, red, out, sl, NT);
+    }
+}
+
+// First-order step: move the result from the stage buffers back to the state.
+template <class R, int NT>
+__global__ void __launch_bounds__(NT) stage_copy_kernel(const Grid<R>* __restrict__ grids,
+                                                         const StripRef* __restrict__ strips,
+                                                         const StepParams* __restrict__ params) {
+    const StripRef sr = strips[blockIdx.x];
+    const Grid<R>& gd = grids[sr.member];
+    if (!params[sr.member].active) return;
+    const int cx = sr.x0 + threadIdx.x;
+    if ((int)threadIdx.x >= sr.w || cx >= gd.nx) return;
+    for (int y = sr.y0; y < sr.y1; ++y) {
+        const size_t i = (size_t)y * gd.nx + cx;
+        gd.h[i] = gd.h1[i];
+        gd.hu[i] = gd.hu1[i];
+        gd.hv[i] = gd.hv1[i];
+    }
+}
+
+// Per strip-chunk CFL rate, surface and retained water of the current state (float64 sums).
+template <class R, int NT>
+__global__ void __launch_bounds__(NT) strip_reduce_kernel(const Grid<R>* __restrict__ grids,
+                                                           const StripRef* __restrict__ strips, const KC<R> c,
+                                                           double* __restrict__ partials) {
+    __shared__ double red[32 * 3];
+    const StripRef sr = strips[blockIdx.x];
+    const Grid<R>& gd = grids[sr.member];
+    double rate = 0, hs = 0, ss = 0;
+    const int cx = sr.x0 + threadIdx.x;
+    if ((int)threadIdx.x < sr.w && cx < gd.nx) {
+        for (int y = sr.y0; y < sr.y1 && y < gd.ny; ++y) {
+            const size_t i = (size_t)y * gd.nx + cx;
+            R h = gd.h[i], u, v;
+            kp_velocity(c, h, gd.hu[i], gd.hv[i], u, v);
+            const R cw = dsqrt(c.g * h);
+            const R r = h > c.h_dry ? (fabs(u) + cw) / gd.rdx + (fabs(v) + cw) / gd.rdy : R(0);
+            rate = fmax(rate, (double)r);
+            hs += (double)h;
+            ss += (double)gd.sf[i];
+        }
+    }
+    double v[3] = {rate, hs, ss};
+    const bool mx[3] = {true, false, false};
+    const int sl[3] = {P_RATE, P_HSUM, P_SSUM};
+    block_reduce_store<3>(v, mx, red, partials + (size_t)blockIdx.x * NPART, sl, NT);
+}
+
+// Per-member totals from the strip-chunk partials, in a fixed order.  out: 8 per
+// member = bnd_in, bnd_out, rain, infil, clip (m^3), rate (1/s), surface and retained
+// volume.  mode 0: after a step; mode 1: rate and volumes only.
+template <class R>
+__global__ void finalize_kernel(const Grid<R>* __restrict__ grids, const StepParams* __restrict__ params, Consts c,
+                                const double* __restrict__ partials, double* __restrict__ out, int mode) {
+    const int m = blockIdx.x, lane = threadIdx.x;
+    const Grid<R>& gd = grids[m];
+    if (mode == 0 && !params[m].active) return;
+    double s[NPART];
+#pragma unroll
+    for (int j = 0; j < NPART; ++j) s[j] = 0.0;
+    for (int t = lane; t < gd.n_tiles; t += 32) {
+        const double* p = partials + (size_t)(gd.tile0 + t) * NPART;
+#pragma unroll
+        for (int j = 0; j < NPART; ++j) s[j] = (j == P_RATE || j == P_HMAX) ? fmax(s[j], p[j]) : s[j] + p[j];
+    }
+#pragma unroll
+    for (int j = 0; j < NPART; ++j) s[j] = (j == P_RATE || j == P_HMAX) ? warp_max(s[j]) : warp_sum(s[j]);
+    if (lane != 0) return;
+    double* o = out + (size_t)m * 8;
+    o[5] = s[P_RATE];
+    o[6] = s[P_HSUM] * gd.area;
+    o[7] = s[P_SSUM] * gd.area;
+    if (mode != 0) return;
+    const StepParams& pr = params[m];
+    const double dt = (double)R(pr.dt);
+    double qin = s[P_XIN1] * gd.dy + s[P_YIN1] * gd.dx;
+    double qout = s[P_XOUT1] * gd.dy + s[P_YOUT1] * gd.dx;
+    double clip = s[P_CLIP1] * gd.area;
+    if (c.order == 2) {
+        double qin2 = s[P_XIN2] * gd.dy + s[P_YIN2] * gd.dx;
+        double qout2 = s[P_XOUT2] * gd.dy + s[P_YOUT2] * gd.dx;
+        qin = 0.5 * (qin + qin2);
+        qout = 0.5 * (qout + qout2);
+        clip = clip + s[P_CLIP2] * gd.area;
+    }
+    o[0] = qin * dt;
+    o[1] = qout * dt;
+    if (gd.rw) o[2] = s[P_RAINW] * gd.area;
+    else o[2] = (double)(R(pr.rain) * R(pr.dt)) * ((double)((long long)gd.nx * gd.ny) * gd.area);
+    o[3] = s[P_INFIL] * gd.area;
+    o[4] = clip;
+}
+
+}  // namespace his

@@ -78,8 +78,9 @@ typedef struct his_links his_links;
 int32_t his_version(void);
 const char* his_last_error(void);
 
-/* Create a set of n_members 2-D grids computed in `precision`.  tile_x/tile_y pick
- * the stencil tile (0, 0 = default); the set allocates its own stage scratch.
+/* Create a set of n_members 2-D grids computed in `precision`.  The stencil kernels
+ * march up strips of at most tile_x columns (1..122) in chunks of tile_y rows
+ * (0, 0 = defaults 58 x 48); the set allocates its own stage scratch.
  * Replaces hydrointel/solver/swe2d.py:113-146 (SWE2D constructor, batched form). */
 int32_t his_grid_create(int32_t precision, const his_solver_cfg* cfg, int32_t n_members, const his_grid_desc* grids,
                         int32_t tile_x, int32_t tile_y, his_grid** out);
