@@ -86,6 +86,8 @@ SIGNATURES = {
     "his_grid_step": (C.c_int32, [_H, C.POINTER(StepParams), _F64P, C.c_void_p]),
     "his_grid_max_rate": (C.c_int32, [_H, _F64P, C.c_void_p]),
     "his_grid_volumes": (C.c_int32, [_H, _F64P, C.c_void_p]),
+    "his_grid_step_noalloc": (C.c_int32, [C.c_int32, C.POINTER(SolverCfg), C.POINTER(GridDesc),
+                                          C.POINTER(StepParams), _F64P, C.c_void_p]),
     "his_net_create": (C.c_int32, [C.POINTER(SolverCfg), C.c_int32, C.POINTER(NetDesc), C.POINTER(_H)]),
     "his_net_destroy": (C.c_int32, [_H]),
     "his_net_step": (C.c_int32, [_H, C.c_double, C.c_int32, _F64P, _F64P, C.c_void_p]),

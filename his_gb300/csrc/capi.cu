@@ -23,7 +23,7 @@ int cuda_fail(cudaError_t e, const char* what) {
 // threads up to 58 columns, 128 up to 122), chunks of ty rows.
 bool tile_supported(int tx, int ty) { return tx >= 1 && tx <= 122 && ty >= 1 && ty <= 1 << 20; }
 
-static Consts to_consts(const his_solver_cfg* c) {
+Consts to_consts(const his_solver_cfg* c) {
     Consts k{};
     k.g = c->g; k.h_dry = c->h_dry; k.kp_eps = c->kp_eps; k.cfl = c->cfl; k.dt_min = c->dt_min; k.dt_max = c->dt_max;
     k.cfl_1d = c->cfl_1d; k.slot_width_frac = c->slot_width_frac; k.weir_cw = c->weir_cw;
@@ -37,7 +37,7 @@ static int bad(const std::string& msg) {
     return HIS_ERR_BAD_ARG;
 }
 
-static int check_cfg(const his_solver_cfg* c) {
+int check_cfg(const his_solver_cfg* c) {
     if (!c) return bad("cfg is NULL");
     if (c->order != 1 && c->order != 2) return bad("order must be 1 or 2");
     if (c->hllc != 0 && c->hllc != 1) return bad("hllc must be 0 or 1");

@@ -81,6 +81,21 @@ int cuda_fail(cudaError_t e, const char* what);
     } while (0)
 
 bool tile_supported(int tx, int ty);
+int check_cfg(const his_solver_cfg* c);
+Consts to_consts(const his_solver_cfg* c);
+
+// Layout of the no-allocation 2-D step's scratch (noalloc.cu): one grid in strips of
+// up to 58 columns and chunks of up to 48 rows, every offset a multiple of 256 bytes
+// from the scratch base.
+struct NoallocPlan {
+    int ns, w, nch, hch, n_strips, pad;
+    size_t plane;                       // one (ny, nx) plane of the compute type
+    size_t o_stage, o_part, o_strips, o_grid, o_params, o_out, total;
+};
+int noalloc_step_f64(const Consts& c, const his_grid_desc& d, const his_step_params& p, const NoallocPlan& L,
+                     unsigned char* base, cudaStream_t s);
+int noalloc_step_f32(const Consts& c, const his_grid_desc& d, const his_step_params& p, const NoallocPlan& L,
+                     unsigned char* base, cudaStream_t s);
 
 // precision-specific entry points (swe2d_f64.cu / swe2d_f32.cu)
 int grid_init_f64(his_grid* g);

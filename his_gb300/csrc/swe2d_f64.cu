@@ -10,4 +10,8 @@ int exchange_f64(his_links* l, const Consts& c, double dt, cudaStream_t s) { ret
 int engine_enqueue_f64(his_engine* e, int n) { return engine_enqueue_impl<double>(e, n); }
 int engine_take_rate_f64(his_engine* e) { return engine_take_rate_impl<double>(e); }
 int engine_profile_f64(his_engine* e, int n, double* ms) { return engine_profile_impl<double>(e, n, ms); }
+int noalloc_step_f64(const Consts& c, const his_grid_desc& d, const his_step_params& p, const NoallocPlan& L,
+                     unsigned char* base, cudaStream_t s) {
+    return noalloc_step_impl<double>(c, d, p, L, base, s);
+}
 }  // namespace his

@@ -275,4 +275,89 @@ int engine_profile_impl(his_engine* E, int n_steps, double* ms) {
     HIS_NT_DISPATCH(eng_profile_nt, R, g, E, n_steps, ms);
 }
 
+// ---------------------------------------------------------------- no-allocation step
+// Writes the grid record, the step parameters and the strip table of one grid into
+// the caller's scratch and clears its partial sums and totals.  The records arrive
+// as kernel arguments, so no host buffer has to outlive the call.
+template <class R>
+__global__ void noalloc_setup_kernel(Grid<R> G, StepParams P, NoallocPlan L, unsigned char* __restrict__ base) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    const int stride = gridDim.x * blockDim.x;
+    auto* strips = reinterpret_cast<StripRef*>(base + L.o_strips);
+    auto* part = reinterpret_cast<double*>(base + L.o_part);
+    for (int b = i; b < L.n_strips; b += stride) {
+        const int sx = b % L.ns, cy = b / L.ns;
+        const int x0 = sx * L.w, y0 = cy * L.hch;
+        strips[b] = StripRef{0, x0, min(L.w, G.nx - x0), y0, min(y0 + L.hch, G.ny), 0};
+    }
+    for (int j = i; j < NPART * L.n_strips; j += stride) part[j] = 0.0;
+    if (i < 8) reinterpret_cast<double*>(base + L.o_out)[i] = 0.0;
+    if (i == 0) {
+        *reinterpret_cast<Grid<R>*>(base + L.o_grid) = G;
+        *reinterpret_cast<StepParams*>(base + L.o_params) = P;
+    }
+}
+
+// One step of one grid with every table and stage buffer in the scratch at `base`
+// (laid out by L): the same strip kernels, decomposition (58-column strips, 48-row
+// chunks) and fixed-order totals as a one-member set created with default tiles.
+template <class R>
+int noalloc_step_impl(const Consts& c, const his_grid_desc& d, const his_step_params& p, const NoallocPlan& L,
+                      unsigned char* base, cudaStream_t s) {
+    constexpr int NT = 64;
+    static_assert(sizeof(Grid<R>) <= 256 && sizeof(StepParams) <= 256, "records exceed their scratch slots");
+    int rc = set_strip_attrs<R, NT>();
+    if (rc) return rc;
+    Grid<R> G{};
+    G.ny = d.ny;
+    G.nx = d.nx;
+    for (int e = 0; e < 4; ++e) G.bc[e] = d.bc[e];
+    G.dx = d.dx;
+    G.dy = d.dy;
+    G.area = d.dx * d.dy;
+    G.t0 = d.horton_t0;
+    G.rdx = R(d.dx);
+    G.rdy = R(d.dy);
+    G.rt0 = R(d.horton_t0);
+    G.tile0 = 0;
+    G.tiles_x = L.ns;
+    G.tiles_y = L.nch;
+    G.n_tiles = L.n_strips;
+    G.h = (R*)d.h; G.hu = (R*)d.hu; G.hv = (R*)d.hv; G.sf = (R*)d.s_filled; G.ic = (R*)d.infil_cum;
+    unsigned char* st = base + L.o_stage;
+    G.h1 = (R*)st; G.hu1 = (R*)(st + L.plane); G.hv1 = (R*)(st + 2 * L.plane);
+    G.z = (const R*)d.z; G.n = (const R*)d.manning; G.S = (const R*)d.storage;
+    G.f0 = (const R*)d.f0; G.fc = (const R*)d.fc; G.k = (const R*)d.k; G.rw = (const R*)d.rain_weight;
+    G.pk = (R*)d.peak_h; G.ps = (R*)d.peak_speed;
+    StepParams P{};
+    P.dt = p.dt;
+    P.t = p.t;
+    P.rain = p.rain;
+    for (int e = 0; e < 4; ++e) {
+        P.bc0[e] = p.bc_t[e];
+        P.bc1[e] = p.bc_t_dt[e];
+    }
+    P.active = 1;
+    params_set_f32(P);
+    const int work = std::max(L.n_strips * (int)NPART, 8);
+    noalloc_setup_kernel<R><<<(work + 255) / 256, 256, 0, s>>>(G, P, L, base);
+    auto* grid = reinterpret_cast<const Grid<R>*>(base + L.o_grid);
+    auto* params = reinterpret_cast<const StepParams*>(base + L.o_params);
+    auto* strips = reinterpret_cast<const StripRef*>(base + L.o_strips);
+    auto* part = reinterpret_cast<double*>(base + L.o_part);
+    auto* out = reinterpret_cast<double*>(base + L.o_out);
+    const KC<R> kc = make_kc<R>(c);
+    const size_t smem = StripGeom<R, NT>::smem_bytes;
+    if (c.order == 2) {
+        strip_kernel<R, NT, 1><<<L.n_strips, NT, smem, s>>>(grid, strips, params, kc, part);
+        strip_kernel<R, NT, 2><<<L.n_strips, NT, smem, s>>>(grid, strips, params, kc, part);
+    } else {
+        strip_kernel<R, NT, 0><<<L.n_strips, NT, smem, s>>>(grid, strips, params, kc, part);
+        stage_copy_kernel<R, NT><<<L.n_strips, NT, 0, s>>>(grid, strips, params);
+    }
+    finalize_kernel<R><<<1, 32, 0, s>>>(grid, params, c, part, out, 0);
+    HIS_CK(cudaGetLastError());
+    return HIS_OK;
+}
+
 }  // namespace his

@@ -104,6 +104,27 @@ int32_t his_grid_max_rate(his_grid* grid, double* rate, void* stream);
  * n_members x 2; synchronises).  Replaces hydrointel/solver/swe2d.py:169-174. */
 int32_t his_grid_volumes(his_grid* grid, double* vols, void* stream);
 
+/* Bytes of the device scratch compiled into the library for his_grid_step_noalloc
+ * (per GPU, held for the life of the process): room for one float64 grid of about
+ * 690,000 cells or one float32 grid of about 1,390,000 cells. */
+#define HIS_NOALLOC_SCRATCH_BYTES (16u * 1024u * 1024u)
+
+/* One SSP-RK2 step of ONE 2-D grid that allocates no device memory, for callers that
+ * may not allocate (an embedding whose host application owns every device allocation,
+ * or a one-off step without creating a grid set).  The grid's arrays are described as
+ * for his_grid_create, in `precision`; params is one step's forcing; the stage buffers,
+ * partial sums and tables live in a fixed library array of HIS_NOALLOC_SCRATCH_BYTES
+ * bytes.  Same kernels, decomposition and results as a one-member grid set created
+ * with default tiles.  Grids too large for the array return HIS_ERR_BAD_ARG.  The first
+ * call on each device (with it current) looks up the array's address and should come
+ * before any stream capture.  Calls share the array: calls that may overlap on the GPU
+ * (two streams, two threads) race on it; order them on one stream.  If vols is
+ * non-NULL it receives the 5 float64 volumes of his_grid_step and the call
+ * synchronises `stream`.
+ * No counterpart in the reference: an allocation-free form of his_grid_step. */
+int32_t his_grid_step_noalloc(int32_t precision, const his_solver_cfg* cfg, const his_grid_desc* grid,
+                              const his_step_params* params, double* vols, void* stream);
+
 /* One member's 1-D channel network (flattened cells and faces; kinds 0 reach,
  * 1 junction, 2 inflow ghost, 3 stage ghost, 4 closed ghost).  Arrays are HOST
  * arrays copied at creation; A and Q are DEVICE float64 state (n_cells each).
