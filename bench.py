@@ -276,7 +276,7 @@ def run_ours(args, world, rank, local):
     traffic = read_traffic()
     out = {"metric": "cell-steps/s", "value": value, "unit": "cell-steps/s", "n_gpus": world, "steps": args.steps,
            "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True, "scaling": "weak",
-           "vs_baseline": None, "dtype": "f32 (f64 accumulators, 1-D network and exchange)",
+           "vs_baseline": None, "dtype": "f32 (f64 accumulators and 1-D network)",
            "data": "synthetic (seeded terrain, forcing and networks)",
            "config": workload_config(members),
            "gpu_launches": LAUNCHES_PER_STEP * args.steps,

@@ -208,7 +208,8 @@ int32_t his_net_create(const his_solver_cfg* cfg, int32_t n_members, const his_n
     if (rc) return rc;
     if (n_members <= 0 || !nets) return bad("need at least one network member");
     Arena ar;
-    struct Offs { size_t kind, gsrc, fl, fr, gsign, ls, li, rs, ri, z, n, dx, b, m, yb, ts, fb, fm, fyb, fts; };
+    struct Offs { size_t kind, gsrc, fl, fr, gsign, ls, li, rs, ri, z, n, dx, b, m, yb, ts, fb, fm, fyb, fts;
+                  size_t zf, dxf, bf, mf, ybf, tsf; };
     std::vector<Offs> offs(n_members);
     size_t smem = 0;
     for (int mb = 0; mb < n_members; ++mb) {
@@ -246,6 +247,13 @@ int32_t his_net_create(const his_solver_cfg* cfg, int32_t n_members, const his_n
         o.z = ar.add(d.z, C); o.n = ar.add(d.manning, C); o.dx = ar.add(d.dx, C);
         o.b = ar.add(d.b, C); o.m = ar.add(d.m, C); o.yb = ar.add(d.yb, C); o.ts = ar.add(d.ts, C);
         o.fb = ar.add(d.fb, F); o.fm = ar.add(d.fm, F); o.fyb = ar.add(d.fyb, F); o.fts = ar.add(d.fts, F);
+        // float32 copies of the static cell geometry for the production form's exchange
+        auto addf = [&](const double* a) {
+            std::vector<float> f(a, a + d.n_cells);
+            return ar.add(f.data(), sizeof(float) * f.size());
+        };
+        o.zf = addf(d.z); o.dxf = addf(d.dx); o.bf = addf(d.b); o.mf = addf(d.m); o.ybf = addf(d.yb);
+        o.tsf = addf(d.ts);
         smem = std::max(smem, net_smem_bytes(d.n_cells, d.n_faces));
     }
     if (smem > 200 * 1024) return bad("network too large for one thread block's shared memory");
@@ -278,6 +286,9 @@ int32_t his_net_create(const his_solver_cfg* cfg, int32_t n_members, const his_n
         n.yb = (const double*)(base + o.yb); n.ts = (const double*)(base + o.ts);
         n.fb = (const double*)(base + o.fb); n.fm = (const double*)(base + o.fm);
         n.fyb = (const double*)(base + o.fyb); n.fts = (const double*)(base + o.fts);
+        n.zf = (const float*)(base + o.zf); n.dxf = (const float*)(base + o.dxf);
+        n.bf = (const float*)(base + o.bf); n.mf = (const float*)(base + o.mf);
+        n.ybf = (const float*)(base + o.ybf); n.tsf = (const float*)(base + o.tsf);
         n.A = d.A; n.Q = d.Q;
     }
     e = cudaMalloc(&N->d_nets, sizeof(Net) * n_members);
@@ -351,7 +362,7 @@ int32_t his_links_create(his_grid* grid, his_net* net, int32_t n_members, const 
     if (n_members != grid->n || n_members != net->n)
         return bad("links, grid and network must have the same number of members");
     Arena ar;
-    struct Offs { size_t c1, inv, uq, zb, len, z2, us, ui, cs, ci; };
+    struct Offs { size_t c1, inv, uq, zb, len, z2, us, ui, cs, ci, zbf, lenf, z2f; };
     std::vector<Offs> offs(n_members);
     size_t smem = 0;
     int total = 0;
@@ -381,6 +392,11 @@ int32_t his_links_create(his_grid* grid, his_net* net, int32_t n_members, const 
         o.inv = ar.add(d.inv, sizeof(int32_t) * d.n_links);
         o.uq = ar.add(uq.data(), sizeof(int32_t) * uq.size());
         o.zb = ar.add(d.zbank, L); o.len = ar.add(d.length, L); o.z2 = ar.add(d.z2, L);
+        auto addf = [&](const double* a) {
+            std::vector<float> f(a, a + d.n_links);
+            return ar.add(f.data(), sizeof(float) * f.size());
+        };
+        o.zbf = addf(d.zbank); o.lenf = addf(d.length); o.z2f = addf(d.z2);
         o.us = ar.add(us.data(), sizeof(int) * us.size()); o.ui = ar.add(ui.data(), sizeof(int) * ui.size());
         o.cs = ar.add(cs.data(), sizeof(int) * cs.size()); o.ci = ar.add(ci.data(), sizeof(int) * ci.size());
         smem = std::max(smem, exchange_smem_bytes(d.n_links, d.n_unique, nc));
@@ -405,6 +421,8 @@ int32_t his_links_create(his_grid* grid, his_net* net, int32_t n_members, const 
         L.cell1d = (const int*)(base + o.c1); L.inv = (const int*)(base + o.inv); L.uniq = (const int*)(base + o.uq);
         L.zbank = (const double*)(base + o.zb); L.length = (const double*)(base + o.len);
         L.z2 = (const double*)(base + o.z2);
+        L.zbank_f = (const float*)(base + o.zbf); L.length_f = (const float*)(base + o.lenf);
+        L.z2_f = (const float*)(base + o.z2f);
         L.ustart = (const int*)(base + o.us); L.uidx = (const int*)(base + o.ui);
         L.cstart = (const int*)(base + o.cs); L.cidx = (const int*)(base + o.ci);
     }

@@ -16,6 +16,8 @@
 
 namespace his {
 
+constexpr int ENG_PRE_THREADS = 512;   // threads of the per-member pre-step CTA
+
 __host__ __device__ inline size_t eng_pre_smem_bytes(size_t exchange_bytes) {
     size_t r = sizeof(double) * 64;
     return exchange_bytes > r ? exchange_bytes : r;
@@ -49,7 +51,8 @@ __global__ void eng_pre_kernel(EngMember* __restrict__ em, StepParams* __restric
     if (nets) {
         double r1 = 0.0;
         bool wet = false;
-        net_rate_dev(nets[m], c, r1, wet, sm);
+        if constexpr (sizeof(R) == 4) net_rate_dev_f32(nets[m], c, r1, wet, sm);
+        else net_rate_dev(nets[m], c, r1, wet, sm);
         if (threadIdx.x == 0) {
             const double dt1 = wet ? fmin(c.cfl_1d / r1, c.dt_max) : c.dt_max;
             const double ns = ceil(dt / dt1 - 1e-9);

@@ -97,6 +97,7 @@ struct Grid {
     const R *z, *n, *S, *f0, *fc, *k, *rw;
     R *pk, *ps;                      // optional running peak depth and speed
     R rdx, rdy, rt0;                 // dx, dy, Horton t0 in the compute type
+    R idx, idy;                      // 1/dx, 1/dy (the float32 kernels multiply instead of dividing)
 };
 
 // Per-member step parameters, in float64 and (for the float32 kernels, which must not
@@ -164,10 +165,30 @@ template <> __device__ __forceinline__ float par_bc<float>(const StepParams& p, 
 }
 
 // ------------------------------------------------------------------ scalar helpers
-template <class R> __device__ __forceinline__ R rmax(R a, R b) { return a > b ? a : (b > a ? b : a); }
-template <class R> __device__ __forceinline__ R rmin(R a, R b) { return a < b ? a : (b < a ? b : a); }
-template <class R> __device__ __forceinline__ R relu(R x) { return x > R(0) ? x : R(0); }
-template <class R> __device__ __forceinline__ R clamp0(R x) { return x < R(0) ? R(0) : x; }
+// float64: the selections of the reference's torch.maximum/minimum/clamp on finite
+// values, spelled out; float32: the native min/max instructions.
+template <class R> __device__ __forceinline__ R rmax(R a, R b) {
+    if constexpr (sizeof(R) == 4) return fmaxf(a, b);
+    else return a > b ? a : (b > a ? b : a);
+}
+template <class R> __device__ __forceinline__ R rmin(R a, R b) {
+    if constexpr (sizeof(R) == 4) return fminf(a, b);
+    else return a < b ? a : (b < a ? b : a);
+}
+template <class R> __device__ __forceinline__ R relu(R x) {
+    if constexpr (sizeof(R) == 4) return fmaxf(x, 0.0f);
+    else return x > R(0) ? x : R(0);
+}
+template <class R> __device__ __forceinline__ R clamp0(R x) {
+    if constexpr (sizeof(R) == 4) return fmaxf(x, 0.0f);
+    else return x < R(0) ? R(0) : x;
+}
+// x / d for a cell spacing d: float64 divides as the reference does; float32
+// multiplies by the reciprocal formed once on the host.
+template <class R> __device__ __forceinline__ R per_len(R x, R d, R inv_d) {
+    if constexpr (sizeof(R) == 4) return x * inv_d;
+    else return x / d;
+}
 
 __device__ __forceinline__ double dsqrt(double x) { return sqrt(x); }
 __device__ __forceinline__ float dsqrt(float x) { return sqrtf(x); }
@@ -187,6 +208,14 @@ __device__ __forceinline__ float cbrt_pow(float x) { return powf(x, 1.0f / 3.0f)
 template <class R>
 __device__ __forceinline__ void kp_velocity(const KC<R>& c, R h, R hu, R hv, R& u, R& v) {
     const R SQRT2 = R(1.4142135623730951);
+    if constexpr (sizeof(R) == 4) {
+        const float h2 = h * h, h4 = h2 * h2;
+        const float s = SQRT2 * h * rsqrtf(h4 + fmaxf(h4, c.kp_eps));
+        const bool wet = h >= c.h_dry;
+        u = wet ? hu * s : 0.0f;
+        v = wet ? hv * s : 0.0f;
+        return;
+    }
     R h4 = pow4(h);
     R den = dsqrt(h4 + rmax(h4, c.kp_eps));
     if (h >= c.h_dry) {

@@ -6,8 +6,12 @@
 // in the reference's index order, so every sum has the reference's association
 // and the result does not depend on thread scheduling.
 //
-// All arithmetic is float64 in both precisions (the 1-D network, its junction level
-// pool and the exchange volumes are the float64 islands of the production form).
+// The 1-D network and its junction level pool are float64 in both precisions (a
+// float64 island of the production form).  The weir exchange is float64 in the
+// plain method; in the production form its per-link arithmetic is float32 (GB300's
+// float64 pipe runs at a small fraction of the float32 rate and this work sits on
+// every step's critical path), with the 1-D area update and the exchanged-volume
+// tallies kept in float64.
 //
 // Reference: hydrointel/solver/swe1d.py:51-107, :253-368; coupling.py:73-124.
 #pragma once
@@ -23,6 +27,7 @@ struct Net {
     const double *z, *nman, *dx;
     const double *b, *m, *yb, *ts;                 // cell sections
     const double *fb, *fm, *fyb, *fts;             // face sections
+    const float *zf, *dxf, *bf, *mf, *ybf, *tsf;   // float32 copies of z, dx and the cell sections
     double *A, *Q;
 };
 
@@ -30,6 +35,7 @@ struct Lnk {
     int n_links, n_unique, v_offset, pad;
     const int *cell1d, *inv, *uniq;
     const double *zbank, *length, *z2;
+    const float *zbank_f, *length_f, *z2_f;        // float32 copies for the production form
     const int *ustart, *uidx;                      // unique 2-D cell -> links (link order)
     const int *cstart, *cidx;                      // 1-D cell -> links (link order)
 };
@@ -248,15 +254,116 @@ __device__ __forceinline__ void net_substeps_dev(const Net& N, const Consts& c, 
 
 
 __host__ __device__ inline size_t exchange_smem_bytes(int n_links, int n_unique, int n_cells) {
-    return sizeof(double) * (2 * (size_t)n_links + 2 * (size_t)n_unique + (size_t)n_cells + 32 * 2);
+    const size_t f64 = sizeof(double) * (2 * (size_t)n_links + 2 * (size_t)n_unique + (size_t)n_cells + 32 * 2);
+    const size_t f32 = sizeof(float) * (2 * (size_t)n_links + 2 * (size_t)n_unique + 4 * (size_t)n_cells) +
+                       sizeof(double) * 32 * 2;
+    return f64 > f32 ? f64 : f32;
 }
 
-// Weir exchange for one member per CTA (coupling.py:73-124).  dt is per member
-// (params) when params is non-NULL, else dt_host.  V: per-link volumes at
-// lnk.v_offset; exch: per member (2-D -> 1-D total, 1-D -> 2-D total).
-template <class R>
-__device__ __forceinline__ void exchange_dev(const Lnk& L, const Net& N, const Grid<R>& gd, const Consts& c, double dt,
-                                             double* __restrict__ Vout, double* __restrict__ exch, int mb, double* sm) {
+// Production-form exchange (2-D state in float32): the same steps as the float64
+// form below, in float32 arithmetic from float32 copies of the static link and
+// section tables.  Per 1-D cell the level, plan width and donor volume are formed
+// once; the 1-D area update and the tallies accumulate in float64.
+__device__ __forceinline__ void exchange_dev_f32(const Lnk& L, const Net& N, const Grid<float>& gd, const Consts& c,
+                                                 double dt, double* __restrict__ Vout, double* __restrict__ exch,
+                                                 int mb, double* sm) {
+    const int nl = L.n_links, nu = L.n_unique, nc = N.n_cells, tid = threadIdx.x, nt = blockDim.x;
+    double* red = sm;                                   // 64 doubles
+    float* V = reinterpret_cast<float*>(sm + 64);
+    float *sg = V + nl, *hu_ = sg + nl, *f2 = hu_ + nu, *eta1 = f2 + nu, *plan1 = eta1 + nc, *f1 = plan1 + nc,
+          *avail1 = f1 + nc;
+    __shared__ float s_k[6];
+    if (tid == 0) {
+        s_k[0] = (float)dt;
+        s_k[1] = (float)c.weir_cw;
+        s_k[2] = (float)c.exchange_relax;
+        s_k[3] = (float)c.exchange_limit;
+        s_k[4] = (float)gd.area;
+        s_k[5] = (float)(1.0 / gd.area);
+    }
+    for (int k = tid; k < nu; k += nt) hu_[k] = gd.h[L.uniq[k]];
+    for (int i = tid; i < nc; i += nt) {
+        const float A = fmaxf((float)N.A[i], 0.0f);
+        const float b = N.bf[i], m = N.mf[i], yb = N.ybf[i], ts = N.tsf[i];
+        const float ab = yb * (b + m * yb);
+        const float y = A <= ab ? 2.0f * A / (b + sqrtf(b * b + 4.0f * m * A)) : yb + (A - ab) / ts;
+        eta1[i] = N.zf[i] + y;
+        plan1[i] = (y <= yb ? b + 2.0f * m * y : ts) * N.dxf[i];
+        avail1[i] = fmaxf(A - ab, 0.0f) * N.dxf[i];
+    }
+    __syncthreads();
+    const float dtf = s_k[0], cw = s_k[1], relax = s_k[2], limit = s_k[3], area2 = s_k[4], rarea2 = s_k[5];
+    for (int l = tid; l < nl; l += nt) {
+        const int c1 = L.cell1d[l];
+        const float eta2 = L.z2_f[l] + hu_[L.inv[l]];
+        const float e1 = eta1[c1];
+        const float zb = L.zbank_f[l];
+        const float up = fmaxf(e1, eta2), dn = fminf(e1, eta2);
+        const float d_up = fmaxf(up - zb, 0.0f), d_dn = fmaxf(dn - zb, 0.0f);
+        const float ratio = d_up > 0.0f ? d_dn / d_up : 0.0f;
+        const float sub = powf(fmaxf(1.0f - ratio * sqrtf(ratio), 0.0f), 0.385f);
+        const float q = cw * L.length_f[l] * (d_up * sqrtf(d_up)) * sub;
+        sg[l] = eta2 > e1 ? 1.0f : -1.0f;
+        const float v_eq = (up - dn) / (rarea2 + 1.0f / plan1[c1]);
+        V[l] = fminf(q * dtf, relax * v_eq);
+    }
+    __syncthreads();
+    // donor limits, aggregated per donor in link order (coupling.py:98-107)
+    for (int k = tid; k < nu; k += nt) {
+        float tot = 0.0f;
+        for (int j = L.ustart[k]; j < L.ustart[k + 1]; ++j) { int l = L.uidx[j]; tot += sg[l] > 0.0f ? V[l] : 0.0f; }
+        const float avail = limit * hu_[k] * area2;
+        f2[k] = tot > avail ? avail / (tot > 0.0f ? tot : 1.0f) : 1.0f;
+    }
+    for (int i = tid; i < nc; i += nt) {
+        float tot = 0.0f;
+        for (int j = L.cstart[i]; j < L.cstart[i + 1]; ++j) { int l = L.cidx[j]; tot += sg[l] < 0.0f ? V[l] : 0.0f; }
+        const float avail = limit * avail1[i];
+        f1[i] = tot > avail ? avail / (tot > 0.0f ? tot : 1.0f) : 1.0f;
+    }
+    __syncthreads();
+    float ex0 = 0.0f, ex1 = 0.0f;
+    for (int l = tid; l < nl; l += nt) {
+        const float v = (sg[l] > 0.0f ? V[l] * f2[L.inv[l]] : V[l] * f1[L.cell1d[l]]) * sg[l];
+        V[l] = v;
+        if (Vout) Vout[L.v_offset + l] = (double)v;
+        ex0 += fmaxf(v, 0.0f);
+        ex1 += fmaxf(-v, 0.0f);
+    }
+    __syncthreads();
+    // apply: 2-D through the unique cells, momentum kept only for water that stays
+    for (int k = tid; k < nu; k += nt) {
+        float d = 0.0f;
+        for (int j = L.ustart[k]; j < L.ustart[k + 1]; ++j) d += V[L.uidx[j]];
+        const float hu0 = hu_[k];
+        const float hn = hu0 - d * rarea2;
+        const float keep = hu0 > 0.0f ? fminf(hn / hu0, 1.0f) : 0.0f;
+        const int idx = L.uniq[k];
+        gd.h[idx] = hn;
+        gd.hu[idx] = gd.hu[idx] * keep;
+        gd.hv[idx] = gd.hv[idx] * keep;
+    }
+    for (int i = tid; i < nc; i += nt) {
+        float d = 0.0f;
+        for (int j = L.cstart[i]; j < L.cstart[i + 1]; ++j) d += V[L.cidx[j]];
+        if (d != 0.0f) N.A[i] = N.A[i] + (double)(d / N.dxf[i]);
+    }
+    double ex[2] = {(double)ex0, (double)ex1};
+    block_sum<2>(ex, red);
+    if (tid == 0 && exch) {
+        exch[mb * 2 + 0] += ex[0];
+        exch[mb * 2 + 1] += ex[1];
+    }
+    __syncthreads();
+}
+
+// Weir exchange for one member per CTA, float64 plain method (coupling.py:73-124).
+// V: per-link volumes at lnk.v_offset; exch: per member (2-D -> 1-D total,
+// 1-D -> 2-D total).
+__device__ __forceinline__ void exchange_dev_f64(const Lnk& L, const Net& N, const Grid<double>& gd, const Consts& c,
+                                                 double dt, double* __restrict__ Vout, double* __restrict__ exch,
+                                                 int mb, double* sm) {
+    using R = double;
     const int nl = L.n_links, nu = L.n_unique, nc = N.n_cells, tid = threadIdx.x, nt = blockDim.x;
     double *V = sm, *sg = V + nl, *hu_ = sg + nl, *f2 = hu_ + nu, *f1 = f2 + nu, *red = f1 + nc;
     const Sec s{N.b, N.m, N.yb, N.ts};
@@ -273,15 +380,7 @@ __device__ __forceinline__ void exchange_dev(const Lnk& L, const Net& N, const G
         const double up = rmax(eta1, eta2), dn = rmin(eta1, eta2);
         const double d_up = clamp0(up - zb), d_dn = clamp0(dn - zb);
         const double ratio = d_up > 0.0 ? d_dn / d_up : 0.0;
-        double q;
-        if constexpr (sizeof(R) == 8) {
-            q = c.weir_cw * L.length[l] * pow(d_up, 1.5) * pow(clamp0(1.0 - pow(ratio, 1.5)), 0.385);
-        } else {
-            // production form: the weir law's powers in float32 (the FP64 pipe is ~1/64 rate)
-            const float df = (float)d_up, rf = (float)ratio;
-            const float sub = powf(fmaxf(1.0f - rf * sqrtf(rf), 0.0f), 0.385f);
-            q = (double)((float)(c.weir_cw * L.length[l]) * (df * sqrtf(df)) * sub);
-        }
+        const double q = c.weir_cw * L.length[l] * pow(d_up, 1.5) * pow(clamp0(1.0 - pow(ratio, 1.5)), 0.385);
         sg[l] = eta2 > eta1 ? 1.0 : -1.0;
         double v = q * dt;
         const double plan1 = (y1 <= N.yb[c1] ? N.b[c1] + 2.0 * N.m[c1] * y1 : N.ts[c1]) * N.dx[c1];
@@ -339,6 +438,13 @@ __device__ __forceinline__ void exchange_dev(const Lnk& L, const Net& N, const G
 }
 
 template <class R>
+__device__ __forceinline__ void exchange_dev(const Lnk& L, const Net& N, const Grid<R>& gd, const Consts& c, double dt,
+                                             double* __restrict__ Vout, double* __restrict__ exch, int mb, double* sm) {
+    if constexpr (sizeof(R) == 4) exchange_dev_f32(L, N, gd, c, dt, Vout, exch, mb, sm);
+    else exchange_dev_f64(L, N, gd, c, dt, Vout, exch, mb, sm);
+}
+
+template <class R>
 __global__ void exchange_kernel(const Lnk* __restrict__ links, const Net* __restrict__ nets,
                                 const Grid<R>* __restrict__ grids, Consts c, double dt, double* __restrict__ Vout,
                                 double* __restrict__ exch) {
@@ -372,6 +478,47 @@ __device__ __forceinline__ void net_rate_dev(const Net& N, const Consts& c, doub
         for (int k = 1; k < nw; ++k) { r = fmax(r, red[k * 2]); w = fmax(w, red[k * 2 + 1]); }
         rate_o = r;
         wet_o = w > 0.0;
+    }
+    __syncthreads();
+}
+
+// The same rate in float32 arithmetic (production form: it only sets the substep count).
+__device__ __forceinline__ void net_rate_dev_f32(const Net& N, const Consts& c, double& rate_o, bool& wet_o,
+                                                 double* red) {
+    __shared__ float s_c[2];
+    if (threadIdx.x == 0) {
+        s_c[0] = (float)c.g;
+        s_c[1] = (float)c.h_dry;
+    }
+    __syncthreads();
+    const float g = s_c[0], h_dry = s_c[1];
+    float rate = 0.0f, wet_any = 0.0f;
+    for (int i = threadIdx.x; i < N.n_cells; i += blockDim.x) {
+        if (N.kind[i] > 1) continue;
+        const float A = fmaxf((float)N.A[i], 0.0f);
+        const float b = N.bf[i], m = N.mf[i], yb = N.ybf[i], ts = N.tsf[i];
+        const float ab = yb * (b + m * yb);
+        const float y = A <= ab ? 2.0f * A / (b + sqrtf(b * b + 4.0f * m * A)) : yb + (A - ab) / ts;
+        if (!(y > h_dry)) continue;
+        wet_any = 1.0f;
+        const float top = y <= yb ? b + 2.0f * m * y : ts;
+        const float cc = sqrtf(g * A / top);
+        const float u = (float)N.Q[i] / fmaxf(A, 1e-12f);
+        rate = fmaxf(rate, (fabsf(u) + cc) / N.dxf[i]);
+    }
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = (blockDim.x + 31) >> 5;
+    for (int o = 16; o > 0; o >>= 1) {
+        rate = fmaxf(rate, __shfl_xor_sync(0xffffffffu, rate, o));
+        wet_any = fmaxf(wet_any, __shfl_xor_sync(0xffffffffu, wet_any, o));
+    }
+    float* redf = reinterpret_cast<float*>(red);
+    if (lane == 0) { redf[warp * 2] = rate; redf[warp * 2 + 1] = wet_any; }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        float r = redf[0], w = redf[1];
+        for (int k = 1; k < nw; ++k) { r = fmaxf(r, redf[k * 2]); w = fmaxf(w, redf[k * 2 + 1]); }
+        rate_o = (double)r;
+        wet_o = w > 0.0f;
     }
     __syncthreads();
 }

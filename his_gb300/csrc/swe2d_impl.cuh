@@ -103,6 +103,8 @@ int grid_init_impl(his_grid* g) {
         G.rdx = R(d.dx);
         G.rdy = R(d.dy);
         G.rt0 = R(d.horton_t0);
+        G.idx = R(1.0 / d.dx);
+        G.idy = R(1.0 / d.dy);
         const int ns = (d.nx + wmax - 1) / wmax;
         const int w = (d.nx + ns - 1) / ns;
         const int nch = (d.ny + g->ty - 1) / g->ty;
@@ -175,7 +177,7 @@ int eng_enqueue_nt(his_grid* g, his_engine* E, int n_steps) {
     const Lnk* links = E->links ? E->links->d_links : nullptr;
     double* exch = E->links ? E->links->d_exch : nullptr;
     for (int k = 0; k < n_steps; ++k) {
-        eng_pre_kernel<R><<<E->n, 256, E->pre_smem, E->s0>>>(E->d_em, g->d_params, grids, nets, links, g->c,
+        eng_pre_kernel<R><<<E->n, ENG_PRE_THREADS, E->pre_smem, E->s0>>>(E->d_em, g->d_params, grids, nets, links, g->c,
                                                              E->d_netf, E->max_sub, exch);
         if (E->net) {
             HIS_CK(cudaEventRecord(E->ev_fork, E->s0));
@@ -228,7 +230,7 @@ int eng_profile_nt(his_grid* g, his_engine* E, int n_steps, double* ms) {
     int rc = HIS_OK;
     for (int k = 0; k < n_steps && rc == HIS_OK; ++k) {
         cudaEventRecord(ev[0], E->s0);
-        eng_pre_kernel<R><<<E->n, 256, E->pre_smem, E->s0>>>(E->d_em, g->d_params, grids, nets, links, g->c,
+        eng_pre_kernel<R><<<E->n, ENG_PRE_THREADS, E->pre_smem, E->s0>>>(E->d_em, g->d_params, grids, nets, links, g->c,
                                                              E->d_netf, E->max_sub, exch);
         cudaEventRecord(ev[1], E->s0);
         if (E->net) {
@@ -319,6 +321,8 @@ int noalloc_step_impl(const Consts& c, const his_grid_desc& d, const his_step_pa
     G.rdx = R(d.dx);
     G.rdy = R(d.dy);
     G.rt0 = R(d.horton_t0);
+    G.idx = R(1.0 / d.dx);
+    G.idy = R(1.0 / d.dy);
     G.tile0 = 0;
     G.tiles_x = L.ns;
     G.tiles_y = L.nch;

@@ -281,7 +281,7 @@ __global__ void __launch_bounds__(NT) strip_kernel(const Grid<R>* __restrict__ g
     const R* __restrict__ H = STAGE == 2 ? gd.h1 : gd.h;
     const R* __restrict__ HU = STAGE == 2 ? gd.hu1 : gd.hu;
     const R* __restrict__ HV = STAGE == 2 ? gd.hv1 : gd.hv;
-    const R rdx = gd.rdx, rdy = gd.rdy;
+    const R rdx = gd.rdx, rdy = gd.rdy, idx = gd.idx, idy = gd.idy;
     const R rdt = par_rain<R>(pr) * dt;
     const R tt = clamp0(par_t<R>(pr) - gd.rt0);
     const bool col_in = (unsigned)cx < (unsigned)nx;
@@ -363,7 +363,7 @@ __global__ void __launch_bounds__(NT) strip_kernel(const Grid<R>* __restrict__ g
                     const int fr = (row & (G::FR - 1)) * NT;
                     const R Fw = s_xf1[fr + t], Fe = s_xf1[fr + t + 1];
                     const R Gs = s_yf1[fr + t], Gn = s_yf1[((row + 1) & (G::FR - 1)) * NT + t];
-                    const R out = (relu(Fe) + relu(-Fw)) / rdx + (relu(Gn) + relu(-Gs)) / rdy;
+                    const R out = per_len(relu(Fe) + relu(-Fw), rdx, idx) + per_len(relu(Gn) + relu(-Gs), rdy, idy);
                     const R need = out * dt;
                     const R hh = s_h[(row & (G::RING - 1)) * NT + t];
                     th = need > hh ? hh / (need > R(0) ? need : R(1)) : R(1);
@@ -383,19 +383,19 @@ __global__ void __launch_bounds__(NT) strip_kernel(const Grid<R>* __restrict__ g
             const R sw = Fw > R(0) ? thW : thC, se = Fe > R(0) ? thC : thE;
             const R ss = Gs > R(0) ? thS : thC, sn = Gn > R(0) ? thC : thN;
             const R F1w = Fw * sw, F1e = Fe * se, G1s = Gs * ss, G1n = Gn * sn;
-            R a1 = -(F1e - F1w) / rdx;
-            R a2 = -(s_xf2l[f0 + t + 1] - s_xf2r[f0 + t]) / rdx;
-            R a3 = -(s_xf3[f0 + t + 1] * se - s_xf3[f0 + t] * sw) / rdx;
-            R b1 = -(G1n - G1s) / rdy;
-            R b2 = -(s_yf2l[f1 + t] - s_yf2r[f0 + t]) / rdy;
-            R b3 = -(s_yf3[f1 + t] * sn - s_yf3[f0 + t] * ss) / rdy;
+            R a1 = per_len(-(F1e - F1w), rdx, idx);
+            R a2 = per_len(-(s_xf2l[f0 + t + 1] - s_xf2r[f0 + t]), rdx, idx);
+            R a3 = per_len(-(s_xf3[f0 + t + 1] * se - s_xf3[f0 + t] * sw), rdx, idx);
+            R b1 = per_len(-(G1n - G1s), rdy, idy);
+            R b2 = per_len(-(s_yf2l[f1 + t] - s_yf2r[f0 + t]), rdy, idy);
+            R b3 = per_len(-(s_yf3[f1 + t] * sn - s_yf3[f0 + t] * ss), rdy, idy);
             const int cm = ((orow - 1) & (G::RING - 1)) * NT + t, c0 = (orow & (G::RING - 1)) * NT + t;
             const int cp = ((orow + 1) & (G::RING - 1)) * NT + t;
             if (c.order == 2) {
                 R scx = bed_source(c, s_h[c0 - 1], s_h[c0], s_h[c0 + 1], s_z[c0 - 1], s_z[c0], s_z[c0 + 1]);
                 R scy = bed_source(c, s_h[cm], s_h[c0], s_h[cp], s_z[cm], s_z[c0], s_z[cp]);
-                a2 = a2 + scx / rdx;
-                b2 = b2 + scy / rdy;
+                a2 = a2 + per_len(scx, rdx, idx);
+                b2 = b2 + per_len(scy, rdy, idy);
             }
             const R dh = a1 + b1, dhu = a2 + b3, dhv = a3 + b2;
             if (cx == 0) { xin += relu(F1w); xout += relu(-F1w); }
@@ -481,7 +481,7 @@ __global__ void __launch_bounds__(NT) strip_kernel(const Grid<R>* __restrict__ g
                 R u2, v2;
                 kp_velocity(c, hn, hun, hvn, u2, v2);
                 const R cw = dsqrt(c.g * hn);
-                const R rr = hn > c.h_dry ? (fabs(u2) + cw) / rdx + (fabs(v2) + cw) / rdy : R(0);
+                const R rr = hn > c.h_dry ? per_len(fabs(u2) + cw, rdx, idx) + per_len(fabs(v2) + cw, rdy, idy) : R(0);
                 rate = rmax(rate, rr);
                 hsum += hn;
                 ssum += sf;
@@ -540,7 +540,8 @@ __global__ void __launch_bounds__(NT) strip_reduce_kernel(const Grid<R>* __restr
             R h = gd.h[i], u, v;
             kp_velocity(c, h, gd.hu[i], gd.hv[i], u, v);
             const R cw = dsqrt(c.g * h);
-            const R r = h > c.h_dry ? (fabs(u) + cw) / gd.rdx + (fabs(v) + cw) / gd.rdy : R(0);
+            const R r = h > c.h_dry ? per_len(fabs(u) + cw, gd.rdx, gd.idx) + per_len(fabs(v) + cw, gd.rdy, gd.idy)
+                                    : R(0);
             rate = fmax(rate, (double)r);
             hs += (double)h;
             ss += (double)gd.sf[i];
