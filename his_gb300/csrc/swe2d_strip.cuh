@@ -30,16 +30,21 @@ struct StripRef {
 // Shared-memory layout of one CTA
 template <class R, int NT>
 struct StripGeom {
-    static constexpr int RING = 8;                 // cell rows kept
-    static constexpr int FR = 4;                   // face / theta rows kept
+    static constexpr int RING = 8;                 // cell rows kept (rows r-4 .. r are live)
+    static constexpr int FR = 4;                   // y-face and theta rows kept (3 live)
+    static constexpr int FRX = 2;                  // x-face rows kept (2 live)
     static constexpr int NREC = 10;                // x-reconstruction values per cell
-    static constexpr int NRED = 11;
+    static constexpr int NRED = 11;                // reduced values (the reduction reuses the cell ring)
     static constexpr size_t cells = (size_t)RING * NT * 4;
     static constexpr size_t xrec = (size_t)NREC * NT;
-    static constexpr size_t xf = (size_t)FR * NT * 4;
+    static constexpr size_t xf = (size_t)FRX * NT * 4;
     static constexpr size_t yf = (size_t)FR * NT * 4;
     static constexpr size_t th = (size_t)FR * NT;
-    static constexpr size_t smem_bytes = sizeof(R) * (cells + xrec + xf + yf + th) + sizeof(R) * 32 * NRED + 32;
+    static_assert(cells >= (size_t)32 * NRED, "reduction scratch must fit in the cell ring");
+    static constexpr size_t smem_bytes = sizeof(R) * (cells + xrec + xf + yf + th);
+    // resident CTAs per SM the float32 kernels are register-capped for (shared memory
+    // allows 12 of 64 threads); float64 keeps the compiler's choice
+    static constexpr int MIN_CTAS = sizeof(R) == 4 ? 768 / NT : 1;
 };
 
 // Bed source of one cell along one axis (swe2d.py:220); float32: the bed source plus
@@ -245,7 +250,7 @@ __device__ __forceinline__ Recon<R> load_recon(const R* xr, int stride, int t) {
 // to the stage buffers and stage_copy_kernel moves it back (no CTA overwrites cells
 // that another CTA may still read).
 template <class R, int NT, int STAGE>
-__global__ void __launch_bounds__(NT) strip_kernel(const Grid<R>* __restrict__ grids,
+__global__ void __launch_bounds__(NT, StripGeom<R, NT>::MIN_CTAS) strip_kernel(const Grid<R>* __restrict__ grids,
                                                     const StripRef* __restrict__ strips,
                                                     const StepParams* __restrict__ params, const KC<R> c,
                                                     double* __restrict__ partials) {
@@ -256,16 +261,16 @@ __global__ void __launch_bounds__(NT) strip_kernel(const Grid<R>* __restrict__ g
     R* s_v = s_u + G::RING * NT;
     R* s_z = s_v + G::RING * NT;
     R* s_xr = s_z + G::RING * NT;                     // [NREC][NT]
-    R* s_xf1 = s_xr + G::NREC * NT;                   // [FR][NT] each
-    R* s_xf2l = s_xf1 + G::FR * NT;
-    R* s_xf2r = s_xf2l + G::FR * NT;
-    R* s_xf3 = s_xf2r + G::FR * NT;
-    R* s_yf1 = s_xf3 + G::FR * NT;
+    R* s_xf1 = s_xr + G::NREC * NT;                   // [FRX][NT] each
+    R* s_xf2l = s_xf1 + G::FRX * NT;
+    R* s_xf2r = s_xf2l + G::FRX * NT;
+    R* s_xf3 = s_xf2r + G::FRX * NT;
+    R* s_yf1 = s_xf3 + G::FRX * NT;                   // [FR][NT] each
     R* s_yf2l = s_yf1 + G::FR * NT;
     R* s_yf2r = s_yf2l + G::FR * NT;
     R* s_yf3 = s_yf2r + G::FR * NT;
     R* s_th = s_yf3 + G::FR * NT;                     // [FR][NT]
-    R* red = reinterpret_cast<R*>((reinterpret_cast<uintptr_t>(s_th + G::FR * NT) + 15) & ~uintptr_t(15));
+    R* red = s_h;                                     // after the row loop
     __shared__ R bcv[4];
 
     const StripRef sr = strips[blockIdx.x];
@@ -352,7 +357,7 @@ __global__ void __launch_bounds__(NT) strip_kernel(const Grid<R>* __restrict__ g
                 Recon<R> L = load_recon(s_xr, NT, t - 1), Rr = load_recon(s_xr, NT, t);
                 R F1, F2L, F2R, F3;
                 face_flux(c, L, Rr, F1, F2L, F2R, F3);
-                const int fs = (row & (G::FR - 1)) * NT + t;
+                const int fs = (row & (G::FRX - 1)) * NT + t;
                 s_xf1[fs] = F1; s_xf2l[fs] = F2L; s_xf2r[fs] = F2R; s_xf3[fs] = F3;
             }
             __syncthreads();
@@ -360,8 +365,8 @@ __global__ void __launch_bounds__(NT) strip_kernel(const Grid<R>* __restrict__ g
             if (do_theta) {
                 R th = R(1);
                 if ((unsigned)row < (unsigned)ny && col_in) {
-                    const int fr = (row & (G::FR - 1)) * NT;
-                    const R Fw = s_xf1[fr + t], Fe = s_xf1[fr + t + 1];
+                    const int fr = (row & (G::FR - 1)) * NT, frx = (row & (G::FRX - 1)) * NT;
+                    const R Fw = s_xf1[frx + t], Fe = s_xf1[frx + t + 1];
                     const R Gs = s_yf1[fr + t], Gn = s_yf1[((row + 1) & (G::FR - 1)) * NT + t];
                     const R out = per_len(relu(Fe) + relu(-Fw), rdx, idx) + per_len(relu(Gn) + relu(-Gs), rdy, idy);
                     const R need = out * dt;
@@ -376,16 +381,17 @@ __global__ void __launch_bounds__(NT) strip_kernel(const Grid<R>* __restrict__ g
         const int orow = r - 3;
         if (orow >= y0 && orow < y1 && do_out) {
             const int f0 = (orow & (G::FR - 1)) * NT, f1 = ((orow + 1) & (G::FR - 1)) * NT;
+            const int fx = (orow & (G::FRX - 1)) * NT;
             const int tc = f0 + t;
             const R thC = s_th[tc], thW = s_th[tc - 1], thE = s_th[tc + 1];
             const R thS = s_th[((orow - 1) & (G::FR - 1)) * NT + t], thN = s_th[f1 + t];
-            const R Fw = s_xf1[f0 + t], Fe = s_xf1[f0 + t + 1], Gs = s_yf1[f0 + t], Gn = s_yf1[f1 + t];
+            const R Fw = s_xf1[fx + t], Fe = s_xf1[fx + t + 1], Gs = s_yf1[f0 + t], Gn = s_yf1[f1 + t];
             const R sw = Fw > R(0) ? thW : thC, se = Fe > R(0) ? thC : thE;
             const R ss = Gs > R(0) ? thS : thC, sn = Gn > R(0) ? thC : thN;
             const R F1w = Fw * sw, F1e = Fe * se, G1s = Gs * ss, G1n = Gn * sn;
             R a1 = per_len(-(F1e - F1w), rdx, idx);
-            R a2 = per_len(-(s_xf2l[f0 + t + 1] - s_xf2r[f0 + t]), rdx, idx);
-            R a3 = per_len(-(s_xf3[f0 + t + 1] * se - s_xf3[f0 + t] * sw), rdx, idx);
+            R a2 = per_len(-(s_xf2l[fx + t + 1] - s_xf2r[fx + t]), rdx, idx);
+            R a3 = per_len(-(s_xf3[fx + t + 1] * se - s_xf3[fx + t] * sw), rdx, idx);
             R b1 = per_len(-(G1n - G1s), rdy, idy);
             R b2 = per_len(-(s_yf2l[f1 + t] - s_yf2r[f0 + t]), rdy, idy);
             R b3 = per_len(-(s_yf3[f1 + t] * sn - s_yf3[f0 + t] * ss), rdy, idy);
