@@ -30,10 +30,10 @@ struct StripRef {
 // Shared-memory layout of one CTA
 template <class R, int NT>
 struct StripGeom {
-    static constexpr int RING = 8;                 // cell rows kept (rows r-4 .. r are live)
+    static constexpr int RING = 6;                 // cell rows kept (rows r-4 .. r are live)
     static constexpr int FR = 4;                   // y-face and theta rows kept (3 live)
     static constexpr int FRX = 2;                  // x-face rows kept (2 live)
-    static constexpr int NREC = 10;                // x-reconstruction values per cell
+    static constexpr int NREC = 8;                 // x-reconstruction values per cell
     static constexpr int NRED = 11;                // reduced values (the reduction reuses the cell ring)
     static constexpr size_t cells = (size_t)RING * NT * 4;
     static constexpr size_t xrec = (size_t)NREC * NT;
@@ -43,8 +43,8 @@ struct StripGeom {
     static_assert(cells >= (size_t)32 * NRED, "reduction scratch must fit in the cell ring");
     static constexpr size_t smem_bytes = sizeof(R) * (cells + xrec + xf + yf + th);
     // resident CTAs per SM the float32 kernels are register-capped for (shared memory
-    // allows 12 of 64 threads); float64 keeps the compiler's choice
-    static constexpr int MIN_CTAS = sizeof(R) == 4 ? 768 / NT : 1;
+    // allows 14 of 64 threads); float64 keeps the compiler's choice
+    static constexpr int MIN_CTAS = sizeof(R) == 4 ? 896 / NT : 1;
 };
 
 // Bed source of one cell along one axis (swe2d.py:220); float32: the bed source plus
@@ -214,6 +214,8 @@ __device__ __forceinline__ void block_reduce_store(T (&v)[NV], const bool* is_ma
     }
 }
 
+// x-reconstruction of one cell in shared memory (8 values); the float32 form's cell
+// depth and bed are read back from the cell ring (hrow, zrow: the cell's row there).
 template <class R>
 __device__ __forceinline__ void store_recon(R* xr, int stride, int t, const Recon<R>& r) {
     xr[0 * stride + t] = r.Hm; xr[1 * stride + t] = r.Hp;
@@ -222,13 +224,12 @@ __device__ __forceinline__ void store_recon(R* xr, int stride, int t, const Reco
     if constexpr (sizeof(R) == 8) {
         xr[6 * stride + t] = r.Zm; xr[7 * stride + t] = r.Zp;
     } else {
-        xr[6 * stride + t] = r.z; xr[7 * stride + t] = r.d;
-        xr[8 * stride + t] = r.h0; xr[9 * stride + t] = r.sE;
+        xr[6 * stride + t] = r.d; xr[7 * stride + t] = r.sE;
     }
 }
 
 template <class R>
-__device__ __forceinline__ Recon<R> load_recon(const R* xr, int stride, int t) {
+__device__ __forceinline__ Recon<R> load_recon(const R* xr, int stride, int t, const R* hrow, const R* zrow) {
     Recon<R> r;
     r.Hm = xr[0 * stride + t]; r.Hp = xr[1 * stride + t];
     r.Um = xr[2 * stride + t]; r.Up = xr[3 * stride + t];
@@ -237,8 +238,8 @@ __device__ __forceinline__ Recon<R> load_recon(const R* xr, int stride, int t) {
         r.Zm = xr[6 * stride + t]; r.Zp = xr[7 * stride + t];
         r.z = r.d = r.h0 = r.sE = R(0);
     } else {
-        r.z = xr[6 * stride + t]; r.d = xr[7 * stride + t];
-        r.h0 = xr[8 * stride + t]; r.sE = xr[9 * stride + t];
+        r.d = xr[6 * stride + t]; r.sE = xr[7 * stride + t];
+        r.z = zrow[t]; r.h0 = hrow[t];
         r.Zm = r.Zp = R(0);
     }
     return r;
@@ -300,21 +301,26 @@ __global__ void __launch_bounds__(NT, StripGeom<R, NT>::MIN_CTAS) strip_kernel(c
     R acc_clip = 0, xin = 0, xout = 0, yin = 0, yout = 0, infil = 0, rainw = 0, rate = 0, hsum = 0, ssum = 0;
     R hmax = 0;
     Recon<R> ylow;                                   // y-reconstruction of row r-2 (carried)
-    // software pipeline: halo rows are fetched two rows ahead, update inputs one row ahead
+    // software pipeline: halo rows are fetched two rows ahead, update inputs at the start
+    // of the iteration that uses them
     HaloRaw<R> ra = halo_fetch(c, gd, H, HU, HV, cx, y0 - 3);
     HaloRaw<R> rb = halo_fetch(c, gd, H, HU, HV, cx, y0 - 2);
     CellIn<R> cin;
+    // ring slot of the current row r (rows r-4 .. r are live in a ring of 6)
+    int s0 = ((y0 - 3) % G::RING + G::RING) % G::RING;
     __syncthreads();
 
     for (int r = y0 - 3; r <= y1 + 2; ++r) {
+        const int s1 = s0 == 0 ? G::RING - 1 : s0 - 1;          // row r-1
+        const int s2 = s1 == 0 ? G::RING - 1 : s1 - 1;          // row r-2
+        const int s3 = s2 == 0 ? G::RING - 1 : s2 - 1;          // row r-3
+        const int s4 = s3 == 0 ? G::RING - 1 : s3 - 1;          // row r-4
         // ---- P1: build row r from values fetched two rows ago; fetch row r + 2 and the
         //      update inputs of row r - 2
-        const int sl = r & (G::RING - 1);
+        const int sl = s0;
         const HaloRaw<R> rnext = halo_fetch(c, gd, H, HU, HV, cx, r + 2);
-        const int nrow = r - 2;
-        const bool fetch_in = do_out && nrow >= y0 && nrow < y1;
-        CellIn<R> cnext;
-        if (fetch_in) cnext = cell_fetch<R, STAGE>(gd, (size_t)nrow * nx + cx);
+        // update inputs of row r-3, consumed after three barriers of this iteration
+        if (do_out && r - 3 >= y0 && r - 3 < y1) cin = cell_fetch<R, STAGE>(gd, (size_t)(r - 3) * nx + cx);
         {
             R hh, uu, vv, zz;
             halo_build(c, gd, bcv, ra, cx, r, hh, uu, vv, zz);
@@ -325,7 +331,7 @@ __global__ void __launch_bounds__(NT, StripGeom<R, NT>::MIN_CTAS) strip_kernel(c
         __syncthreads();
         // ---- P2: y-face between rows r-2 and r-1 (face index r-1), x-reconstruction of row r-2
         if (r >= y0 - 1) {
-            const int a = (r - 2) & (G::RING - 1), b = (r - 1) & (G::RING - 1), cslot = r & (G::RING - 1);
+            const int a = s2, b = s1, cslot = s0;
             if (do_yface) {
                 // y-reconstruction of row r-1: normal v, tangential u
                 Recon<R> yup = reconstruct(c, s_h[a * NT + t], s_h[b * NT + t], s_h[cslot * NT + t],
@@ -342,7 +348,7 @@ __global__ void __launch_bounds__(NT, StripGeom<R, NT>::MIN_CTAS) strip_kernel(c
                 ylow = yup;
             }
             if (r >= y0 + 1 && do_xrec) {
-                const int rr = ((r - 2) & (G::RING - 1)) * NT;
+                const int rr = s2 * NT;
                 Recon<R> xr = reconstruct(c, s_h[rr + t - 1], s_h[rr + t], s_h[rr + t + 1], s_u[rr + t - 1],
                                           s_u[rr + t], s_u[rr + t + 1], s_v[rr + t - 1], s_v[rr + t],
                                           s_v[rr + t + 1], s_z[rr + t - 1], s_z[rr + t], s_z[rr + t + 1]);
@@ -354,7 +360,9 @@ __global__ void __launch_bounds__(NT, StripGeom<R, NT>::MIN_CTAS) strip_kernel(c
             const int row = r - 2;
             // ---- P3: x-faces of row r-2 (face cx between columns cx-1 and cx)
             if (do_xface && (unsigned)row < (unsigned)ny) {
-                Recon<R> L = load_recon(s_xr, NT, t - 1), Rr = load_recon(s_xr, NT, t);
+                const R* hrow = s_h + s2 * NT;
+                const R* zrow = s_z + s2 * NT;
+                Recon<R> L = load_recon(s_xr, NT, t - 1, hrow, zrow), Rr = load_recon(s_xr, NT, t, hrow, zrow);
                 R F1, F2L, F2R, F3;
                 face_flux(c, L, Rr, F1, F2L, F2R, F3);
                 const int fs = (row & (G::FRX - 1)) * NT + t;
@@ -370,7 +378,7 @@ __global__ void __launch_bounds__(NT, StripGeom<R, NT>::MIN_CTAS) strip_kernel(c
                     const R Gs = s_yf1[fr + t], Gn = s_yf1[((row + 1) & (G::FR - 1)) * NT + t];
                     const R out = per_len(relu(Fe) + relu(-Fw), rdx, idx) + per_len(relu(Gn) + relu(-Gs), rdy, idy);
                     const R need = out * dt;
-                    const R hh = s_h[(row & (G::RING - 1)) * NT + t];
+                    const R hh = s_h[s2 * NT + t];
                     th = need > hh ? hh / (need > R(0) ? need : R(1)) : R(1);
                 }
                 s_th[(row & (G::FR - 1)) * NT + t] = th;
@@ -395,8 +403,7 @@ __global__ void __launch_bounds__(NT, StripGeom<R, NT>::MIN_CTAS) strip_kernel(c
             R b1 = per_len(-(G1n - G1s), rdy, idy);
             R b2 = per_len(-(s_yf2l[f1 + t] - s_yf2r[f0 + t]), rdy, idy);
             R b3 = per_len(-(s_yf3[f1 + t] * sn - s_yf3[f0 + t] * ss), rdy, idy);
-            const int cm = ((orow - 1) & (G::RING - 1)) * NT + t, c0 = (orow & (G::RING - 1)) * NT + t;
-            const int cp = ((orow + 1) & (G::RING - 1)) * NT + t;
+            const int cm = s4 * NT + t, c0 = s3 * NT + t, cp = s2 * NT + t;
             if (c.order == 2) {
                 R scx = bed_source(c, s_h[c0 - 1], s_h[c0], s_h[c0 + 1], s_z[c0 - 1], s_z[c0], s_z[c0 + 1]);
                 R scy = bed_source(c, s_h[cm], s_h[c0], s_h[cp], s_z[cm], s_z[c0], s_z[cp]);
@@ -494,7 +501,7 @@ __global__ void __launch_bounds__(NT, StripGeom<R, NT>::MIN_CTAS) strip_kernel(c
                 hmax = rmax(hmax, hn);
             }
         }
-        if (fetch_in) cin = cnext;
+        s0 = s0 == G::RING - 1 ? 0 : s0 + 1;
     }
     __syncthreads();
     double* out = partials + (size_t)blockIdx.x * NPART;
