@@ -47,6 +47,7 @@ def parse():
     p.add_argument("--members", type=int, default=64)
     p.add_argument("--storm-seconds", type=float, default=45.0, help="wall budget of the storms/hour legs")
     p.add_argument("--cpu-seconds", type=float, default=10.0)
+    p.add_argument("--serve-seconds", type=float, default=60.0, help="arrival window of the serving leg")
     p.add_argument("--quick", action="store_true")
     return p.parse_args()
 
@@ -200,6 +201,41 @@ def cpu_oracle_rate(storm, seconds: float, threads: int):
     return {"value": storm.cells * steps / wall, "steps": steps, "wall_s": wall}
 
 
+def uneven_leg(budget_s: float):
+    """48 storms of three grid sizes and their own durations in one engine (one launch per
+    stage over every member's strips, per-member dt, tuned decomposition), run to the end."""
+    import numpy as np
+    from his_gb300 import workloads as W
+    from his_gb300.config import SolverConfig
+    from his_gb300.engine import FloodEngine
+    storms = W.batched_uneven(16)
+    eng = FloodEngine(storms, SolverConfig(), precision="fp32", graph_steps=16)
+    sr = storm_rate(eng, budget_s)
+    cell_steps = sum(s.cells * st for s, st in zip(storms, sr["steps"]))
+    out = {"workload": "batched uneven: 16 x 100x81 @ 80 m + 16 x 200x163 @ 40 m + 16 x 400x325 @ 20 m, "
+                       "durations U(1, 6) h, coupled, per-member dt", "members": len(storms),
+           "tile": list(eng.tile), "storms_per_hour": sr["storms_per_hour"], "completed": sr["completed"],
+           "wall_s": sr["wall_s"], "cell_steps_per_s": cell_steps / sr["wall_s"],
+           "steps_min_max": [int(np.min(sr["steps"])), int(np.max(sr["steps"]))]}
+    if sr["completed"]:
+        out["mass_error_max"] = max(r.mass_error for r in eng.results())
+    return out
+
+
+def serving_leg(window_s: float):
+    """Poisson arrivals (2 requests/s over the window) of storms drawn from the three grid
+    sizes with durations U(0.5, 6) h, served in real time by the continuous-batching loop;
+    latency is arrival to result."""
+    from his_gb300.serving import FloodServer, request_stream
+    reqs = request_stream(2.0, window_s)
+    srv = FloodServer(precision="fp32", chunk_steps=256, tile=(58, 48))
+    st = srv.serve(reqs, max_wall_s=window_s + 240.0)
+    d = dict(st.__dict__)
+    d["workload"] = (f"served: Poisson 2 req/s over {window_s:.0f} s, grids 100x81 @ 80 m / 200x163 @ 40 m / "
+                     "400x325 @ 20 m, durations U(0.5, 6) h, fp32, admission by HBM footprint")
+    return d
+
+
 def e2e_dropin(storms, steps: int):
     """Same metric through the drop-in public API (batched CoupledEngine -> C ABI, host
     buffers): every step uploads its forcing and downloads its volumes and CFL rates."""
@@ -310,6 +346,11 @@ def run_ours(args, world, rank, local):
         out["speedup_vs_plain_fp64_single"] = out["storms_per_hour"] / pr["storms_per_hour"]
         del pe
         torch.cuda.empty_cache()
+        out["uneven_batch"] = uneven_leg(args.storm_seconds)
+        torch.cuda.empty_cache()
+        if args.serve_seconds > 0:
+            out["serving"] = serving_leg(args.serve_seconds)
+            torch.cuda.empty_cache()
         out["e2e"] = e2e_dropin(storms[: min(members, 64)], steps=20)
         threads = os.cpu_count() or 1
         cpu = cpu_oracle_rate(storms[0], args.cpu_seconds, threads)

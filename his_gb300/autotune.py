@@ -1,0 +1,162 @@
+"""Work-decomposition tuner of the 2-D stage kernels.
+
+The strip kernels split every member's grid into strips of at most ``tile_x``
+columns (a 64-thread CTA up to 58 columns, a 128-thread CTA up to 122) and chunks
+of at most ``tile_y`` rows (``his_grid_create``).  The fastest split depends on the
+grid sizes, the batch and the precision: narrow strips recompute more halo
+columns, short chunks more halo rows, and the number of strip-chunks decides how
+evenly the CTAs fill the GPU (152 SMs, 14 resident 64-thread CTAs each in float32).
+
+``choose_tile`` times ``his_grid_step`` for every candidate on throw-away copies of
+the members' state (the fields are shared read-only), keeps the fastest and caches
+the choice per device, precision, spatial order and batch shape, in memory and in a
+JSON file (``$HIS_GB300_TUNE_CACHE``, default ``~/.cache/his_gb300/tiles.json``).
+
+The decomposition changes only the order in which the volume partials are summed
+(in the compute type within a strip-chunk, in float64 across them), never a cell's
+arithmetic: every candidate gives the same state.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import json
+import os
+import threading
+from collections import Counter
+from pathlib import Path
+
+import numpy as np
+import torch
+
+from . import _lib
+
+CANDIDATES_X = (58, 122)
+CANDIDATES_Y = (16, 24, 32, 40, 48, 64, 96, 128)
+WARMUP_STEPS = 2
+TIMED_STEPS = 3
+
+_MEM: dict[str, tuple[int, int]] = {}
+_LOCK = threading.Lock()
+
+
+def cache_path() -> Path:
+    p = os.environ.get("HIS_GB300_TUNE_CACHE")
+    return Path(p) if p else Path.home() / ".cache" / "his_gb300" / "tiles.json"
+
+
+def tune_key(device: torch.device, prec: int, order: int, shapes: list[tuple[int, int]]) -> str:
+    name = torch.cuda.get_device_name(device)
+    hist = sorted(Counter(shapes).items())
+    return f"{name}|prec{prec}|o{order}|" + ";".join(f"{ny}x{nx}*{k}" for (ny, nx), k in hist)
+
+
+def _load_file() -> dict:
+    try:
+        return json.loads(cache_path().read_text())
+    except (OSError, ValueError):
+        return {}
+
+
+def _store_file(key: str, tile: tuple[int, int], times: dict) -> None:
+    p = cache_path()
+    try:
+        p.parent.mkdir(parents=True, exist_ok=True)
+        data = _load_file()
+        data[key] = {"tile": list(tile), "ms": times}
+        tmp = p.with_suffix(f".{os.getpid()}.tmp")
+        tmp.write_text(json.dumps(data, indent=1, sort_keys=True))
+        os.replace(tmp, p)
+    except OSError:
+        pass                                   # a read-only home only loses the cache
+
+
+def candidates(shapes: list[tuple[int, int]]) -> list[tuple[int, int]]:
+    """Distinct decompositions: candidates that give the same strips and chunks for every
+    member are timed once."""
+    seen, out = set(), []
+    for tx in CANDIDATES_X:
+        for ty in CANDIDATES_Y:
+            sig = []
+            for ny, nx in set(shapes):
+                ns = -(-nx // tx)
+                nch = -(-ny // ty)
+                sig.append((ny, nx, -(-nx // ns), -(-ny // nch), tx <= 58))
+            sig = tuple(sorted(sig))
+            if sig not in seen:
+                seen.add(sig)
+                out.append((tx, ty))
+    return out
+
+
+def _time_candidate(lib, prec, cfgc, descs, n, tile, params, stream) -> float:
+    g = C.c_void_p()
+    _lib.check(lib.his_grid_create(prec, C.byref(cfgc), n, descs, tile[0], tile[1], C.byref(g)), "his_grid_create")
+    try:
+        for _ in range(WARMUP_STEPS):
+            _lib.check(lib.his_grid_step(g, params, None, stream.cuda_stream), "his_grid_step")
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        for _ in range(TIMED_STEPS):
+            _lib.check(lib.his_grid_step(g, params, None, stream.cuda_stream), "his_grid_step")
+        e1.record(stream)
+        e1.synchronize()
+        return e0.elapsed_time(e1) / TIMED_STEPS
+    finally:
+        lib.his_grid_destroy(g)
+
+
+def choose_tile(device: torch.device, prec: int, cfg, descs, states: list[list[torch.Tensor]],
+                use_cache: bool = True) -> tuple[int, int]:
+    """Fastest (tile_x, tile_y) for a grid set described by ``descs`` (GridDesc array)
+    whose per-member state tensors are ``states[b] = [h, hu, hv, s_filled, infil_cum]``."""
+    n = len(states)
+    shapes = [(int(descs[b].ny), int(descs[b].nx)) for b in range(n)]
+    key = tune_key(device, prec, int(cfg.spatial_order), shapes)
+    with _LOCK:
+        if use_cache:
+            if key in _MEM:
+                return _MEM[key]
+            hit = _load_file().get(key)
+            if hit:
+                _MEM[key] = tuple(hit["tile"])
+                return _MEM[key]
+        lib = _lib.load()
+        cfgc = _lib.solver_cfg(cfg)
+        copies = []
+        tdesc = (_lib.GridDesc * n)()
+        with torch.cuda.device(device):
+            for b in range(n):
+                c = [x.clone() for x in states[b]]
+                copies.append(c)
+                d = _lib.GridDesc.from_buffer_copy(descs[b])
+                d.h, d.hu, d.hv, d.s_filled, d.infil_cum = (x.data_ptr() for x in c)
+                d.peak_h = d.peak_speed = None
+                tdesc[b] = d
+            # a representative step: each member's own CFL step of its current state
+            probe = C.c_void_p()
+            _lib.check(lib.his_grid_create(prec, C.byref(cfgc), n, tdesc, 0, 0, C.byref(probe)), "his_grid_create")
+            rate = np.zeros(n)
+            stream = torch.cuda.current_stream(device)
+            try:
+                _lib.check(lib.his_grid_max_rate(probe, _lib.as_p(rate), stream.cuda_stream), "his_grid_max_rate")
+            finally:
+                lib.his_grid_destroy(probe)
+            params = (_lib.StepParams * n)()
+            for b in range(n):
+                dt = cfg.cfl / rate[b] if rate[b] > 0 else cfg.dt_max
+                params[b].dt = float(min(max(dt, cfg.dt_min), cfg.dt_max))
+                params[b].t = 0.0
+                params[b].rain = 1e-5
+            times = {}
+            for tile in candidates(shapes):
+                times[f"{tile[0]}x{tile[1]}"] = _time_candidate(lib, prec, cfgc, tdesc, n, tile, params, stream)
+        del copies
+        best = min(times, key=times.get)
+        tile = tuple(int(v) for v in best.split("x"))
+        _MEM[key] = tile
+        if use_cache:
+            _store_file(key, tile, times)
+        return tile
+
+
+__all__ = ["choose_tile", "candidates", "tune_key", "cache_path"]

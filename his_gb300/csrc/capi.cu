@@ -626,6 +626,32 @@ int32_t his_engine_report(his_engine* E, his_member_report* reports, void* strea
     return HIS_OK;
 }
 
+int32_t his_engine_resume(his_engine* E, const his_member_report* reports, const int32_t* mask, void* stream) {
+    if (!E || !reports) return bad("engine and reports are required");
+    for (int m = 0; m < E->n; ++m) {
+        if (mask && !mask[m]) continue;
+        const his_member_report& r = reports[m];
+        if (!std::isfinite(r.t) || r.steps < 0 || r.status < ST_RUNNING || r.status > ST_SUBSTEPS)
+            return bad("member " + std::to_string(m) + ": report has a bad clock, step count or status");
+    }
+    cudaStream_t caller = (cudaStream_t)stream;
+    HIS_CK(cudaEventRecord(E->ev_in, caller));
+    HIS_CK(cudaStreamWaitEvent(E->s0, E->ev_in, 0));
+    HIS_CK(cudaMemcpyAsync(E->h_em, E->d_em, sizeof(EngMember) * E->n, cudaMemcpyDeviceToHost, E->s0));
+    HIS_CK(cudaStreamSynchronize(E->s0));
+    for (int m = 0; m < E->n; ++m) {
+        if (mask && !mask[m]) continue;
+        const his_member_report& r = reports[m];
+        EngMember& M = E->h_em[m];
+        M.t = r.t; M.dt = r.dt_last; M.dt_min = r.dt_min; M.dt_max = r.dt_max; M.rate = r.rate;
+        M.steps = r.steps; M.status = r.status; M.n_sub_max = r.n_sub_max; M.n_clamped = r.n_dt_clamped;
+        for (int j = 0; j < 7; ++j) M.acc[j] = r.acc[j];
+    }
+    HIS_CK(cudaMemcpyAsync(E->d_em, E->h_em, sizeof(EngMember) * E->n, cudaMemcpyHostToDevice, E->s0));
+    HIS_CK(cudaStreamSynchronize(E->s0));
+    return HIS_OK;
+}
+
 int32_t his_engine_profile(his_engine* E, int32_t n_steps, double* ms, void* stream) {
     if (!E || !ms) return bad("engine and ms are required");
     if (n_steps < 0) return bad("n_steps must be >= 0");

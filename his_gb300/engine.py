@@ -8,12 +8,16 @@ This is the production form of the reference's engine assembly and time loop
 its own CFL time step (the reference shares the smallest one across a batch,
 swe2d.py:177-184), and members of different grid sizes share one launch.  A member
 run alone and the same member in a batch execute identical arithmetic in the same
-order, so their results are bit-identical.
+order, so their states are bit-identical.
+
+A storm's device resources (state, fields, channel network, peaks) belong to a
+``Member``; an engine is built over a list of members and can be rebuilt over
+another list (members joining or leaving a batch), each continuing member resuming
+its clock and accumulators exactly (``his_engine_resume``).
 """
 from __future__ import annotations
 
 import ctypes as C
-import math
 import time
 from dataclasses import dataclass
 
@@ -45,154 +49,247 @@ class MemberResult:
     mass_error: float
 
 
+def _report_copy(r) -> _lib.MemberReport:
+    out = _lib.MemberReport()
+    C.memmove(C.byref(out), C.byref(r), C.sizeof(_lib.MemberReport))
+    return out
+
+
+class Member:
+    """One storm's device-resident state and tables, in the engine's precision."""
+
+    def __init__(self, storm: Storm, dtype: torch.dtype, device: torch.device, couple: bool = True,
+                 track_peaks: bool = False, zcache: dict | None = None):
+        self.storm = storm
+        self.key = storm.key
+        self.dtype = dtype
+        self.device = device
+        ter = storm.terrain
+        ny, nx = ter.ny, ter.nx
+        self.shape = (ny, nx)
+        T = lambda a: torch.as_tensor(np.ascontiguousarray(a), dtype=dtype, device=device)
+        if zcache is not None and id(ter) in zcache:
+            self.z = zcache[id(ter)]
+        else:
+            self.z = T(ter.z)
+            if zcache is not None:
+                zcache[id(ter)] = self.z
+        s = storm
+        self.n = T(np.broadcast_to(np.asarray(s.manning, dtype=float), (ny, nx)))
+        self.S = T(s.storage) if s.storage is not None else None
+        self.f0 = self.fc = self.k = None
+        if s.horton is not None:
+            self.f0, self.fc, self.k = (T(np.broadcast_to(s.horton[j], (ny, nx))) for j in range(3))
+        self.h = T(s.h0())
+        self.hu, self.hv, self.s_filled, self.infil_cum = (torch.zeros_like(self.h) for _ in range(4))
+        self.peak_h = self.h.clone() if track_peaks else None
+        self.peak_speed = torch.zeros_like(self.h) if track_peaks else None
+        self.coupled = couple and s.network is not None
+        self.A = self.Q = self.topo = None
+        self.n_links = 0
+        if self.coupled:
+            self._build_network()
+        self._forcing_arrays = (_lib.host_array(s.forcing.rain, np.float64), _lib.host_array(s.forcing.q, np.float64))
+        self.record: _lib.MemberReport | None = None     # clock and accumulators to resume from
+        self.volume0: float | None = None
+
+    @property
+    def cells(self) -> int:
+        return self.shape[0] * self.shape[1]
+
+    def state(self) -> list[torch.Tensor]:
+        return [self.h, self.hu, self.hv, self.s_filled, self.infil_cum]
+
+    def nbytes(self) -> int:
+        """Device bytes held by this member (state, fields, peaks, network), plus the
+        stage scratch and tables a grid set allocates for it."""
+        ts = [self.z, self.n, self.S, self.f0, self.fc, self.k, self.h, self.hu, self.hv, self.s_filled,
+              self.infil_cum, self.peak_h, self.peak_speed, self.A, self.Q]
+        held = sum(t.numel() * t.element_size() for t in ts if t is not None)
+        return held + 3 * self.h.numel() * self.h.element_size() + 64 * 1024
+
+    # ---------------------------------------------------------------- descriptors
+    def _build_network(self):
+        s = self.storm
+        tp = build_topology(s.network)
+        sec = sections(tp, s.slot_width_frac)
+        f = s.forcing
+        yn = normal_depth(tp, sec, f.inflow(0.0))
+        level = np.maximum(tp.z + yn, f.tide(0.0))
+        y = np.maximum(level - tp.z, 0.0)
+        yt = np.minimum(y, sec["yb"])
+        A0 = yt * (sec["b"] + sec["m"] * yt) + sec["ts"] * np.maximum(y - sec["yb"], 0.0)
+        self.A = torch.as_tensor(A0, dtype=torch.float64, device=self.device)
+        self.Q = torch.zeros_like(self.A)
+        self.topo = tp
+        arrs = {k: _lib.host_array(getattr(tp, k), np.int32) for k in ("kind", "ghost_src", "face_l", "face_r")}
+        arrs.update({"ghost_sign": _lib.host_array(tp.ghost_sign, np.float64),
+                     "z": _lib.host_array(tp.z, np.float64), "manning": _lib.host_array(tp.n, np.float64),
+                     "dx": _lib.host_array(tp.dx, np.float64)})
+        arrs.update({k: _lib.host_array(v, np.float64) for k, v in sec.items()})
+        self._net_arrays = arrs
+        cell1d, cells2d, length = bank_links(s.terrain, tp)
+        uniq, inv = np.unique(cells2d, return_inverse=True)
+        self._link_arrays = {
+            "cell1d": _lib.host_array(cell1d, np.int32), "inv": _lib.host_array(inv, np.int32),
+            "uniq": _lib.host_array(uniq, np.int64), "zbank": _lib.host_array(tp.zbank[cell1d], np.float64),
+            "length": _lib.host_array(np.full(len(cell1d), length), np.float64),
+            "z2": _lib.host_array(s.terrain.z.reshape(-1)[cells2d], np.float64)}
+        self.n_links = len(cell1d)
+
+    def fill_grid(self, d) -> None:
+        s = self.storm
+        d.ny, d.nx = self.shape
+        for e, kind in enumerate(s.bc):
+            d.bc[e] = KIND_CODE[kind]
+        d.dx = d.dy = s.terrain.dx
+        d.horton_t0 = float(s.horton[3]) if s.horton is not None else 0.0
+        d.h, d.hu, d.hv, d.s_filled, d.infil_cum = (x.data_ptr() for x in self.state())
+        d.z, d.manning = self.z.data_ptr(), self.n.data_ptr()
+        d.storage = self.S.data_ptr() if self.S is not None else None
+        d.f0 = self.f0.data_ptr() if self.f0 is not None else None
+        d.fc = self.fc.data_ptr() if self.fc is not None else None
+        d.k = self.k.data_ptr() if self.k is not None else None
+        d.rain_weight = None
+        d.peak_h = self.peak_h.data_ptr() if self.peak_h is not None else None
+        d.peak_speed = self.peak_speed.data_ptr() if self.peak_speed is not None else None
+
+    def fill_net(self, d) -> None:
+        tp = self.topo
+        d.n_cells, d.n_faces = tp.n_cells, tp.n_faces
+        for k, v in self._net_arrays.items():
+            setattr(d, k, _lib.as_p(v))
+        d.A, d.Q = self.A.data_ptr(), self.Q.data_ptr()
+
+    def fill_links(self, d) -> None:
+        la = self._link_arrays
+        d.n_links, d.n_unique = len(la["cell1d"]), len(la["uniq"])
+        for k, v in la.items():
+            setattr(d, k, _lib.as_p(v))
+
+    def fill_forcing(self, d) -> None:
+        s = self.storm
+        f = s.forcing
+        rain, q = self._forcing_arrays
+        d.t0, d.t_end = 0.0, float(s.t_end)
+        d.rain_t0, d.rain_step, d.rain_n = f.rain_t0, f.rain_step, len(rain)
+        d.rain = _lib.as_p(rain) if len(rain) else None
+        d.tide_on, d.tide_n = int(bool(f.tide_on)), len(f.tide_amp)
+        d.tide_base, d.tide_shift = f.tide_base, f.tide_shift
+        for j in range(len(f.tide_amp)):
+            d.tide_amp[j], d.tide_w[j], d.tide_phase[j] = f.tide_amp[j], f.tide_w[j], f.tide_phase[j]
+        d.q_t0, d.q_step, d.q_n = f.q_t0, f.q_step, len(q)
+        d.q = _lib.as_p(q) if len(q) else None
+        for e, kind in enumerate(s.bc):
+            d.edge_src[e] = 1 if kind == "stage" else 0
+            d.edge_val[e] = 0.0
+
+
 class FloodEngine:
-    def __init__(self, storms: list[Storm], cfg: SolverConfig | None = None, precision: str = "fp32",
-                 device=None, tile=None, graph_steps: int = 16, max_sub: int = 64, couple: bool = True,
+    def __init__(self, storms: list, cfg: SolverConfig | None = None, precision: str = "fp32",
+                 device=None, tile="auto", graph_steps: int = 16, max_sub: int = 64, couple: bool = True,
                  track_peaks: bool = False):
+        """storms: Storm objects (new members) or Member objects (members moved from
+        another engine, resumed from their records).  tile: (tile_x, tile_y) strip width
+        and chunk height of the 2-D kernels, (0, 0) or None for the defaults, "auto"
+        (default) to let the autotuner measure the candidates for this batch (cached per
+        device, precision and batch shape)."""
         if not storms:
             raise ValueError("FloodEngine needs at least one storm")
         self.cfg = cfg or SolverConfig()
         self.cfg.precision = precision
         self.cfg.validate()
-        self.storms = list(storms)
-        self.B = len(storms)
         self.device = cuda_device(device)
         self.dtype = torch.float64 if precision == "fp64" else torch.float32
         self.prec = _lib.PREC_F64 if precision == "fp64" else _lib.PREC_F32
         self._lib = _lib.load()
-        dev, dt_ = self.device, self.dtype
-        T = lambda a: torch.as_tensor(np.ascontiguousarray(a), dtype=dt_, device=dev)
-        self.h, self.hu, self.hv, self.s_filled, self.infil_cum = [], [], [], [], []
-        self.peak_h, self.peak_speed = [], []
-        self._keep = []
-        zcache = {}
-        gdesc = (_lib.GridDesc * self.B)()
-        for b, s in enumerate(storms):
-            ter = s.terrain
-            ny, nx = ter.ny, ter.nx
-            if id(ter) not in zcache:
-                zcache[id(ter)] = T(ter.z)
-            z = zcache[id(ter)]
-            n = T(np.broadcast_to(np.asarray(s.manning, dtype=float), (ny, nx)))
-            S = T(s.storage) if s.storage is not None else None
-            f0 = fc = kk = None
-            if s.horton is not None:
-                f0, fc, kk = T(np.broadcast_to(s.horton[0], (ny, nx))), T(np.broadcast_to(s.horton[1], (ny, nx))), \
-                    T(np.broadcast_to(s.horton[2], (ny, nx)))
-            h = T(s.h0())
-            st = [h, torch.zeros_like(h), torch.zeros_like(h), torch.zeros_like(h), torch.zeros_like(h)]
-            for lst, x in zip((self.h, self.hu, self.hv, self.s_filled, self.infil_cum), st):
-                lst.append(x)
-            self._keep += [z, n, S, f0, fc, kk]
-            d = gdesc[b]
-            d.ny, d.nx = ny, nx
-            for e, kind in enumerate(s.bc):
-                d.bc[e] = KIND_CODE[kind]
-            d.dx = d.dy = ter.dx
-            d.horton_t0 = float(s.horton[3]) if s.horton is not None else 0.0
-            d.h, d.hu, d.hv, d.s_filled, d.infil_cum = (x.data_ptr() for x in st)
-            d.z, d.manning = z.data_ptr(), n.data_ptr()
-            d.storage = S.data_ptr() if S is not None else None
-            d.f0 = f0.data_ptr() if f0 is not None else None
-            d.fc = fc.data_ptr() if fc is not None else None
-            d.k = kk.data_ptr() if kk is not None else None
-            d.rain_weight = None
-            if track_peaks:
-                pk, ps = h.clone(), torch.zeros_like(h)
-                self.peak_h.append(pk)
-                self.peak_speed.append(ps)
-                d.peak_h, d.peak_speed = pk.data_ptr(), ps.data_ptr()
-            else:
-                d.peak_h = d.peak_speed = None
         self._grid = C.c_void_p()
-        cfgc = _lib.solver_cfg(self.cfg)
-        tx, ty = tile if tile is not None else (0, 0)
-        with torch.cuda.device(dev):
-            _lib.check(self._lib.his_grid_create(self.prec, C.byref(cfgc), self.B, gdesc, int(tx), int(ty),
-                                                 C.byref(self._grid)), "his_grid_create")
         self._net = C.c_void_p()
         self._links = C.c_void_p()
-        self.coupled = couple and all(s.network is not None for s in storms)
-        self.A, self.Q, self.topos = [], [], []
-        if self.coupled:
-            self._build_network(cfgc)
-        self._build_engine(graph_steps, max_sub)
-        self.volume0 = self.volumes()
-
-    # ------------------------------------------------------------------ set-up
-    def _build_network(self, cfgc):
-        ndesc = (_lib.NetDesc * self.B)()
-        ldesc = (_lib.LinksDesc * self.B)()
-        for b, s in enumerate(self.storms):
-            tp = build_topology(s.network)
-            sec = sections(tp, s.slot_width_frac)
-            f = s.forcing
-            yn = normal_depth(tp, sec, f.inflow(0.0))
-            level = np.maximum(tp.z + yn, f.tide(0.0))
-            y = np.maximum(level - tp.z, 0.0)
-            yt = np.minimum(y, sec["yb"])
-            A0 = yt * (sec["b"] + sec["m"] * yt) + sec["ts"] * np.maximum(y - sec["yb"], 0.0)
-            A = torch.as_tensor(A0, dtype=torch.float64, device=self.device)
-            Q = torch.zeros_like(A)
-            self.A.append(A)
-            self.Q.append(Q)
-            self.topos.append(tp)
-            arrs = {k: _lib.host_array(getattr(tp, k), np.int32) for k in ("kind", "ghost_src", "face_l", "face_r")}
-            arrs.update({"ghost_sign": _lib.host_array(tp.ghost_sign, np.float64),
-                         "z": _lib.host_array(tp.z, np.float64), "manning": _lib.host_array(tp.n, np.float64),
-                         "dx": _lib.host_array(tp.dx, np.float64)})
-            arrs.update({k: _lib.host_array(v, np.float64) for k, v in sec.items()})
-            self._keep.append(arrs)
-            d = ndesc[b]
-            d.n_cells, d.n_faces = tp.n_cells, tp.n_faces
-            for k, v in arrs.items():
-                setattr(d, k, _lib.as_p(v))
-            d.A, d.Q = A.data_ptr(), Q.data_ptr()
-            cell1d, cells2d, length = bank_links(s.terrain, tp)
-            uniq, inv = np.unique(cells2d, return_inverse=True)
-            la = {"cell1d": _lib.host_array(cell1d, np.int32), "inv": _lib.host_array(inv, np.int32),
-                  "uniq": _lib.host_array(uniq, np.int64), "zbank": _lib.host_array(tp.zbank[cell1d], np.float64),
-                  "length": _lib.host_array(np.full(len(cell1d), length), np.float64),
-                  "z2": _lib.host_array(s.terrain.z.reshape(-1)[cells2d], np.float64)}
-            self._keep.append(la)
-            ld = ldesc[b]
-            ld.n_links, ld.n_unique = len(cell1d), len(uniq)
-            for k, v in la.items():
-                setattr(ld, k, _lib.as_p(v))
-        with torch.cuda.device(self.device):
-            _lib.check(self._lib.his_net_create(C.byref(cfgc), self.B, ndesc, C.byref(self._net)), "his_net_create")
-            _lib.check(self._lib.his_links_create(self._grid, self._net, self.B, ldesc, C.byref(self._links)),
-                       "his_links_create")
-        self.n_links = [int(ldesc[b].n_links) for b in range(self.B)]
-
-    def _build_engine(self, graph_steps, max_sub):
-        fdesc = (_lib.ForcingDesc * self.B)()
-        for b, s in enumerate(self.storms):
-            f = s.forcing
-            d = fdesc[b]
-            d.t0, d.t_end = 0.0, float(s.t_end)
-            rain = _lib.host_array(f.rain, np.float64)
-            q = _lib.host_array(f.q, np.float64)
-            self._keep += [rain, q]
-            d.rain_t0, d.rain_step, d.rain_n = f.rain_t0, f.rain_step, len(rain)
-            d.rain = _lib.as_p(rain) if len(rain) else None
-            d.tide_on, d.tide_n = int(bool(f.tide_on)), len(f.tide_amp)
-            d.tide_base, d.tide_shift = f.tide_base, f.tide_shift
-            for j in range(len(f.tide_amp)):
-                d.tide_amp[j], d.tide_w[j], d.tide_phase[j] = f.tide_amp[j], f.tide_w[j], f.tide_phase[j]
-            d.q_t0, d.q_step, d.q_n = f.q_t0, f.q_step, len(q)
-            d.q = _lib.as_p(q) if len(q) else None
-            for e, kind in enumerate(s.bc):
-                d.edge_src[e] = 1 if kind == "stage" else 0
-                d.edge_val[e] = 0.0
         self._engine = C.c_void_p()
+        zcache = {}
+        members = []
+        for s in storms:
+            if isinstance(s, Member):
+                if s.dtype != self.dtype or s.device != self.device:
+                    raise ValueError(f"member {s.key} was built for {s.dtype} on {s.device}")
+                members.append(s)
+            else:
+                members.append(Member(s, self.dtype, self.device, couple, track_peaks, zcache))
+        self.members = members
+        self.storms = [m.storm for m in members]
+        self.B = len(members)
+        self.coupled = all(m.coupled for m in members)
+        if any(m.coupled for m in members) and not self.coupled:
+            raise ValueError("a batch is either fully coupled (every storm has a network) or not coupled")
+        gdesc = (_lib.GridDesc * self.B)()
+        for b, m in enumerate(members):
+            m.fill_grid(gdesc[b])
+        cfgc = _lib.solver_cfg(self.cfg)
+        if isinstance(tile, str):
+            if tile != "auto":
+                raise ValueError(f"tile must be (tile_x, tile_y), None or 'auto' (got {tile!r})")
+            from .autotune import choose_tile
+            tile = choose_tile(self.device, self.prec, self.cfg, gdesc, [m.state() for m in members])
+        self.tile = tuple(tile) if tile is not None else (0, 0)
+        tx, ty = self.tile
         with torch.cuda.device(self.device):
+            _lib.check(self._lib.his_grid_create(self.prec, C.byref(cfgc), self.B, gdesc, int(tx), int(ty),
+                                                 C.byref(self._grid)), "his_grid_create")
+            if self.coupled:
+                ndesc = (_lib.NetDesc * self.B)()
+                ldesc = (_lib.LinksDesc * self.B)()
+                for b, m in enumerate(members):
+                    m.fill_net(ndesc[b])
+                    m.fill_links(ldesc[b])
+                _lib.check(self._lib.his_net_create(C.byref(cfgc), self.B, ndesc, C.byref(self._net)),
+                           "his_net_create")
+                _lib.check(self._lib.his_links_create(self._grid, self._net, self.B, ldesc, C.byref(self._links)),
+                           "his_links_create")
+            fdesc = (_lib.ForcingDesc * self.B)()
+            for b, m in enumerate(members):
+                m.fill_forcing(fdesc[b])
             _lib.check(self._lib.his_engine_create(self._grid, self._net if self.coupled else None,
                                                    self._links if self.coupled else None, self.B, fdesc,
                                                    int(max_sub), int(graph_steps), C.byref(self._engine)),
                        "his_engine_create")
+            if any(m.record is not None for m in members):
+                reps = (_lib.MemberReport * self.B)()
+                mask = np.zeros(self.B, dtype=np.int32)
+                for b, m in enumerate(members):
+                    if m.record is not None:
+                        reps[b] = m.record
+                        mask[b] = 1
+                _lib.check(self._lib.his_engine_resume(self._engine, reps, _lib.as_p(mask), _lib.stream_handle()),
+                           "his_engine_resume")
+        if any(m.volume0 is None for m in members):
+            vol = self.volumes()
+            for b, m in enumerate(members):
+                if m.volume0 is None:
+                    m.volume0 = float(vol[b])
+        self.n_links = [m.n_links for m in members] if self.coupled else []
+
+    # ------------------------------------------------------- per-member views
+    h = property(lambda s: [m.h for m in s.members])
+    hu = property(lambda s: [m.hu for m in s.members])
+    hv = property(lambda s: [m.hv for m in s.members])
+    s_filled = property(lambda s: [m.s_filled for m in s.members])
+    infil_cum = property(lambda s: [m.infil_cum for m in s.members])
+    peak_h = property(lambda s: [m.peak_h for m in s.members])
+    peak_speed = property(lambda s: [m.peak_speed for m in s.members])
+    A = property(lambda s: [m.A for m in s.members])
+    Q = property(lambda s: [m.Q for m in s.members])
+    topos = property(lambda s: [m.topo for m in s.members])
+
+    @property
+    def volume0(self) -> np.ndarray:
+        return np.array([m.volume0 for m in self.members])
 
     def __del__(self):
+        self.close()
+
+    def close(self) -> None:
+        """Free the engine's device tables (the members keep their state)."""
         L = _lib._LIB
         if L is None:
             return
@@ -203,10 +300,19 @@ class FloodEngine:
                 getattr(L, fn)(h)
                 setattr(self, attr, C.c_void_p())
 
+    def detach(self) -> list[Member]:
+        """Save every member's record for a later resume, free the engine and return the
+        members (to be placed in another engine)."""
+        reps = self.reports()
+        for m, r in zip(self.members, reps):
+            m.record = _report_copy(r)
+        self.close()
+        return self.members
+
     # ------------------------------------------------------------------ running
     @property
     def cells(self) -> list[int]:
-        return [s.cells for s in self.storms]
+        return [m.cells for m in self.members]
 
     def advance(self, n_steps: int) -> None:
         with torch.cuda.device(self.device):
@@ -249,19 +355,19 @@ class FloodEngine:
                 v = v + v1
         return v
 
-    def results(self) -> list[MemberResult]:
-        reps = self.reports()
+    def results(self, reps=None) -> list[MemberResult]:
+        reps = self.reports() if reps is None else reps
         vol = self.volumes()
         out = []
-        for b, (s, r) in enumerate(zip(self.storms, reps)):
+        for b, (m, r) in enumerate(zip(self.members, reps)):
             src = {k: float(r.acc[j]) for j, k in enumerate(TERMS)}
             net = src["rain"] - src["infiltration"] + src["bnd2d_in"] - src["bnd2d_out"] + src["bnd1d_in"] - \
                 src["bnd1d_out"]
             gross = src["rain"] + src["infiltration"] + src["bnd2d_in"] + src["bnd2d_out"] + src["bnd1d_in"] + \
                 src["bnd1d_out"]
-            v0 = float(self.volume0[b])
+            v0 = float(m.volume0)
             err = abs((float(vol[b]) - v0) - net) / max(gross, 1e-9 * abs(v0) + 1.0)
-            out.append(MemberResult(s.key, _lib.STATUS.get(r.status, str(r.status)), r.t, int(r.steps), r.dt_min,
+            out.append(MemberResult(m.key, _lib.STATUS.get(r.status, str(r.status)), r.t, int(r.steps), r.dt_min,
                                     r.dt_max, r.n_sub_max, r.n_dt_clamped, src, v0, float(vol[b]), err))
         return out
 
@@ -277,4 +383,4 @@ class FloodEngine:
         return errs
 
 
-__all__ = ["FloodEngine", "MemberResult"]
+__all__ = ["FloodEngine", "Member", "MemberResult"]

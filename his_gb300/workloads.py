@@ -90,7 +90,7 @@ def alternating_block(duration_s: float, step_s: float, peak_mmh: float, positio
     i(d) = 1 / (d + 10 min)^0.75, blocks placed alternately about the peak position
     and rescaled so the peak block is ``peak_mmh`` (the block arrangement of the
     reference's hyetograph.alternating_block, hyetograph.py:58-81)."""
-    n = int(round(duration_s / step_s))
+    n = max(1, int(round(duration_s / step_s)))          # a storm shorter than a block is one block
     d = step_s / 60.0 * np.arange(1, n + 1)
     cum = d / (d + 10.0) ** 0.75
     blocks = np.diff(np.concatenate([[0.0], cum]))
@@ -175,9 +175,14 @@ def make_terrain(nx: int, ny: int, dx: float, n_hills: int, key: str, network: s
         paths["trib"] = trib[np.hypot(trib[:, 0] - xj, trib[:, 1] - yj) > dx]
         polylines.append(trib)
     carved = np.zeros((ny, nx), dtype=bool)
+    r = int(np.ceil(half / dx)) + 1            # the disc of each point lies in this window
     for pl in polylines:
         for px, py in pl[:: max(1, len(pl) // 400)]:
-            carved |= np.hypot(X - px, Y - py) < half
+            i0, j0 = int(px / dx), int(py / dx)
+            ia, ib = max(i0 - r, 0), min(i0 + r + 1, nx)
+            ja, jb = max(j0 - r, 0), min(j0 + r + 1, ny)
+            if ia < ib and ja < jb:
+                carved[ja:jb, ia:ib] |= np.hypot(X[ja:jb, ia:ib] - px, Y[ja:jb, ia:ib] - py) < half
     # the main channel is also carved row by row, so no row is skipped on coarse grids
     carved |= np.abs(X - _centreline_x(Y, lx, ly)) < half
     z_plain = z.copy()

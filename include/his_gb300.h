@@ -238,6 +238,15 @@ int32_t his_engine_advance(his_engine* engine, int32_t n_steps, void* stream);
 /* Per-member reports (host out, n_members; synchronises). */
 int32_t his_engine_report(his_engine* engine, his_member_report* reports, void* stream);
 
+/* Continue members from earlier reports: clock, last/min/max dt, CFL rate, step
+ * count, status, substep and clamp statistics and the seven accumulators are set from
+ * reports[m] for every member with mask[m] != 0 (mask NULL = all), so a member moved
+ * into a new engine (another batch) carries on exactly where it stopped; its state
+ * arrays are the ones its descriptors point to.  Synchronises.
+ * Replaces the restart of hydrointel/solver/coupling.py:244-286 (CoupledEngine.run
+ * with t0 and an existing MassBalance). */
+int32_t his_engine_resume(his_engine* engine, const his_member_report* reports, const int32_t* mask, void* stream);
+
 /* Run n_steps steps without graphs, bracketing each kernel class with CUDA events on
  * the stream it is launched on, and return the summed device milliseconds per class:
  * ms[0] pre (dt, exchange, forcing), ms[1] 2-D stage 1, ms[2] 2-D stage 2 + sources,

@@ -1,0 +1,52 @@
+"""Host logic of the decomposition tuner and the serving loop (no GPU)."""
+import json
+
+import numpy as np
+import torch
+
+from his_gb300 import autotune as A
+from his_gb300 import workloads as W
+from his_gb300.serving import estimate_bytes
+
+
+def test_candidates_are_distinct_decompositions():
+    shapes = [(81, 100)] * 4 + [(325, 400)]
+    cands = A.candidates(shapes)
+    assert (58, 16) in cands and len(cands) == len(set(cands))
+    sigs = set()
+    for tx, ty in cands:
+        sig = []
+        for ny, nx in sorted(set(shapes)):
+            ns, nch = -(-nx // tx), -(-ny // ty)
+            sig.append((-(-nx // ns), -(-ny // nch), tx <= 58))
+        sigs.add(tuple(sig))
+    assert len(sigs) == len(cands)
+    # a chunk height above every grid's row count collapses to one candidate per width
+    tall = A.candidates([(10, 30)])
+    assert len(tall) == 2
+
+
+def test_tune_cache_round_trip(tmp_path, monkeypatch):
+    monkeypatch.setenv("HIS_GB300_TUNE_CACHE", str(tmp_path / "tiles.json"))
+    A._store_file("dev|prec1|o2|81x100*4", (58, 24), {"58x24": 0.1, "58x48": 0.2})
+    data = json.loads((tmp_path / "tiles.json").read_text())
+    assert data["dev|prec1|o2|81x100*4"]["tile"] == [58, 24]
+    assert A._load_file()["dev|prec1|o2|81x100*4"]["ms"]["58x48"] == 0.2
+
+
+def test_footprint_estimate_covers_the_state():
+    s = W.uneven_member("fp/0", 2, 3600.0)
+    b32 = estimate_bytes(s, torch.float32)
+    b64 = estimate_bytes(s, torch.float64)
+    assert b32 >= 16 * s.cells * 4
+    assert b64 > 1.9 * b32 - 1e6
+    assert estimate_bytes(s, torch.float32, track_peaks=False) < b32
+
+
+def test_request_stream_is_seeded():
+    a = W.served_requests(2.0, 30.0, key="srv-test")
+    b = W.served_requests(2.0, 30.0, key="srv-test")
+    assert a == b and len(a) > 20
+    t = np.array([x[0] for x in a])
+    assert np.all(np.diff(t) > 0) and t[-1] <= 30.0
+    assert {x[1] for x in a} <= {0, 1, 2}
