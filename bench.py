@@ -49,6 +49,7 @@ def parse():
     p.add_argument("--cpu-seconds", type=float, default=10.0)
     p.add_argument("--serve-seconds", type=float, default=60.0, help="arrival window of the serving leg")
     p.add_argument("--quick", action="store_true")
+    p.add_argument("--tile", default="auto", help="strip width x chunk height of the 2-D kernels, or auto")
     return p.parse_args()
 
 
@@ -280,7 +281,8 @@ def run_ours(args, world, rank, local):
     members = args.members
     storms = W.batched_uniform(members)
     cells = sum(s.cells for s in storms)
-    eng = FloodEngine(storms, SolverConfig(), precision="fp32", graph_steps=16)
+    tile = "auto" if args.tile == "auto" else tuple(int(v) for v in args.tile.split("x"))
+    eng = FloodEngine(storms, SolverConfig(), precision="fp32", graph_steps=16, tile=tile)
     eng.advance(args.warmup)
     torch.cuda.synchronize()
     s = torch.cuda.current_stream()
@@ -315,7 +317,7 @@ def run_ours(args, world, rank, local):
            "vs_baseline": None, "dtype": "f32 (f64 accumulators and 1-D network)",
            "data": "synthetic (seeded terrain, forcing and networks)",
            "config": workload_config(members),
-           "gpu_launches": LAUNCHES_PER_STEP * args.steps,
+           "gpu_launches": LAUNCHES_PER_STEP * args.steps, "tile": list(eng.tile),
            "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s",
                         "frac": achieved / hbm, "peak_kind": peak_kind,
                         "traffic": traffic * cells if traffic is not None else None,
