@@ -7,9 +7,11 @@ tight targets.  Stated tolerances: 1e-9 relative for the 1-row dam breaks and th
 smooth hump; 1e-6 relative for the multi-thousand-step cases (first-order Thacker,
 bump, plane, coupling).  Second-order Thacker is looser: its L2 error after one to
 three periods of a moving wet/dry front is sensitive to last-bit differences (MUSCL
-limiter switching), and the reference itself rerun eagerly on a CPU gives
-[0.0098517, 0.0125181, 0.0160961] for the field bowl against its recorded
-[0.0098512, 0.0125325, 0.0161036] (1.2e-3 apart), so the bound there is 1e-2.
+limiter switching), and the reference itself, rerun eagerly on a CPU, differs from
+its own record: field bowl [0.0098517, 0.0125181, 0.0160961] against the recorded
+[0.0098512, 0.0125325, 0.0161036] (1.2e-3 apart); lab bowl with a 1e-6 m dry
+threshold [0.0095544, 0.0127834, 0.0170633] against [0.0095542, 0.0126227,
+0.0168723] (1.3e-2 apart).  The bounds there are 1e-2 and 3e-2.
 """
 import json
 from pathlib import Path
@@ -54,8 +56,10 @@ def test_thacker_reproduces_recorded_errors():
     m = thacker()
     rec = REC["4"]["metrics"]
     _close(m["field_o1_relL2_per_period"], rec["field_o1_relL2_per_period"], 1e-6, "thacker field_o1")
-    for name in ("field_o2_relL2_per_period", "lab_o2_relL2_per_period", "lab_o2_hdry1e-6_relL2_per_period"):
+    for name in ("field_o2_relL2_per_period", "lab_o2_relL2_per_period"):
         _close(m[name], rec[name], 1e-2, f"thacker {name}")
+    _close(m["lab_o2_hdry1e-6_relL2_per_period"], rec["lab_o2_hdry1e-6_relL2_per_period"], 3e-2,
+           "thacker lab_o2_hdry1e-6")
     assert m["field_o2_mass_err"] < 1e-10 and m["passed"]
 
 
