@@ -273,12 +273,22 @@ __global__ void __launch_bounds__(NT, StripGeom<R, NT>::MIN_CTAS) strip_kernel(c
     R* s_th = s_yf3 + G::FR * NT;                     // [FR][NT]
     R* red = s_h;                                     // after the row loop
     __shared__ R bcv[4];
+    // the member's record, staged once: its field pointers are re-read every row, and
+    // from global memory those reads stall the row loop
+    __shared__ __align__(16) Grid<R> s_gd;
 
     const StripRef sr = strips[blockIdx.x];
-    const Grid<R>& gd = grids[sr.member];
     const StepParams& pr = params[sr.member];
     if (!pr.active) return;
     const int t = threadIdx.x;
+    {
+        static_assert(sizeof(Grid<R>) % 4 == 0, "record copied as 32-bit words");
+        const unsigned* src = reinterpret_cast<const unsigned*>(grids + sr.member);
+        unsigned* dst = reinterpret_cast<unsigned*>(&s_gd);
+        for (int k = t; k < (int)(sizeof(Grid<R>) / 4); k += NT) dst[k] = src[k];
+    }
+    __syncthreads();
+    const Grid<R>& gd = s_gd;
     const int nx = gd.nx, ny = gd.ny;
     const int x0 = sr.x0, W = sr.w, y0 = sr.y0, y1 = sr.y1;
     const int cx = x0 - 3 + t;                        // this thread's column
