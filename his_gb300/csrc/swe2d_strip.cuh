@@ -30,7 +30,7 @@ struct StripRef {
 // Shared-memory layout of one CTA
 template <class R, int NT>
 struct StripGeom {
-    static constexpr int RING = 6;                 // cell rows kept (rows r-4 .. r are live)
+    static constexpr int RING = 4;                 // cell rows kept (rows r-3 .. r are live)
     static constexpr int FR = 4;                   // y-face and theta rows kept (3 live)
     static constexpr int FRX = 2;                  // x-face rows kept (2 live)
     static constexpr int NREC = 8;                 // x-reconstruction values per cell
@@ -47,24 +47,15 @@ struct StripGeom {
     static constexpr int MIN_CTAS = sizeof(R) == 4 ? 896 / NT : 1;
 };
 
-// Bed source of one cell along one axis (swe2d.py:220); float32: the bed source plus
-// the hydrostatic part of the face momentum fluxes, -g/2 (H+ + H-) sE (see riemann_wb).
+// Centred bed source of one cell along one axis (swe2d.py:220), from the cell's own
+// reconstruction: -g/2 (H- + H+)(Z+ - Z-).  float32: Z+ - Z- is the in-cell surface
+// slope sE (the hydrostatic part of the face momentum fluxes is carried by riemann_wb).
+// The row loop computes it where the reconstruction is formed and carries it in
+// registers to the update of that cell.
 template <class R>
-__device__ __forceinline__ R bed_source(const KC<R>& c, R hm, R h0, R hp, R zm, R z0, R zp) {
-    R hmin = rmin(rmin(hm, h0), hp);
-    R ok = (hmin >= c.h_dry) ? R(1) : R(0);
-    R sH = minmod(h0 - hm, hp - h0) * ok;
-    R Hm = h0 - R(0.5) * sH, Hp = h0 + R(0.5) * sH;
-    if constexpr (sizeof(R) == 8) {
-        R em = hm + zm, e0 = h0 + z0, ep = hp + zp;
-        R sE = minmod(e0 - em, ep - e0) * ok;
-        R Em = e0 - R(0.5) * sE, Ep = e0 + R(0.5) * sE;
-        R Zm = Em - Hm, Zp = Ep - Hp;
-        return c.nhg * (Hm + Hp) * (Zp - Zm);
-    } else {
-        R sE = minmod((h0 - hm) + (z0 - zm), (hp - h0) + (zp - z0)) * ok;
-        return c.nhg * (Hm + Hp) * sE;
-    }
+__device__ __forceinline__ R bed_term(const KC<R>& c, const Recon<R>& r) {
+    if constexpr (sizeof(R) == 8) return c.nhg * (r.Hm + r.Hp) * (r.Zp - r.Zm);
+    else return c.nhg * (r.Hm + r.Hp) * r.sE;
 }
 
 // One halo position: an interior cell, or the ghost that the x-sweep (outside in x)
@@ -311,20 +302,19 @@ __global__ void __launch_bounds__(NT, StripGeom<R, NT>::MIN_CTAS) strip_kernel(c
     R acc_clip = 0, xin = 0, xout = 0, yin = 0, yout = 0, infil = 0, rainw = 0, rate = 0, hsum = 0, ssum = 0;
     R hmax = 0;
     Recon<R> ylow;                                   // y-reconstruction of row r-2 (carried)
+    R by1 = R(0), by2 = R(0);                        // y bed terms of rows r-2 and r-3
+    R bxc = R(0);                                    // x bed term of row r-3
     // software pipeline: halo rows are fetched two rows ahead, update inputs at the start
     // of the iteration that uses them
     HaloRaw<R> ra = halo_fetch(c, gd, H, HU, HV, cx, y0 - 3);
     HaloRaw<R> rb = halo_fetch(c, gd, H, HU, HV, cx, y0 - 2);
     CellIn<R> cin;
-    // ring slot of the current row r (rows r-4 .. r are live in a ring of 6)
-    int s0 = ((y0 - 3) % G::RING + G::RING) % G::RING;
+    static_assert((G::RING & (G::RING - 1)) == 0, "ring slots are row & (RING - 1)");
     __syncthreads();
 
     for (int r = y0 - 3; r <= y1 + 2; ++r) {
-        const int s1 = s0 == 0 ? G::RING - 1 : s0 - 1;          // row r-1
-        const int s2 = s1 == 0 ? G::RING - 1 : s1 - 1;          // row r-2
-        const int s3 = s2 == 0 ? G::RING - 1 : s2 - 1;          // row r-3
-        const int s4 = s3 == 0 ? G::RING - 1 : s3 - 1;          // row r-4
+        const int s0 = r & (G::RING - 1), s1 = (r - 1) & (G::RING - 1);   // ring slots of rows r, r-1,
+        const int s2 = (r - 2) & (G::RING - 1), s3 = (r - 3) & (G::RING - 1);  // r-2 and r-3
         // ---- P1: build row r from values fetched two rows ago; fetch row r + 2 and the
         //      update inputs of row r - 2
         const int sl = s0;
@@ -340,6 +330,7 @@ __global__ void __launch_bounds__(NT, StripGeom<R, NT>::MIN_CTAS) strip_kernel(c
         rb = rnext;
         __syncthreads();
         // ---- P2: y-face between rows r-2 and r-1 (face index r-1), x-reconstruction of row r-2
+        R by_new = R(0), bx_new = R(0);
         if (r >= y0 - 1) {
             const int a = s2, b = s1, cslot = s0;
             if (do_yface) {
@@ -356,6 +347,7 @@ __global__ void __launch_bounds__(NT, StripGeom<R, NT>::MIN_CTAS) strip_kernel(c
                     s_yf1[fs] = F1; s_yf2l[fs] = F2L; s_yf2r[fs] = F2R; s_yf3[fs] = F3;
                 }
                 ylow = yup;
+                if (c.order == 2) by_new = bed_term(c, yup);
             }
             if (r >= y0 + 1 && do_xrec) {
                 const int rr = s2 * NT;
@@ -363,6 +355,7 @@ __global__ void __launch_bounds__(NT, StripGeom<R, NT>::MIN_CTAS) strip_kernel(c
                                           s_u[rr + t], s_u[rr + t + 1], s_v[rr + t - 1], s_v[rr + t],
                                           s_v[rr + t + 1], s_z[rr + t - 1], s_z[rr + t], s_z[rr + t + 1]);
                 store_recon(s_xr, NT, t, xr);
+                if (c.order == 2) bx_new = bed_term(c, xr);
             }
         }
         __syncthreads();
@@ -413,12 +406,10 @@ __global__ void __launch_bounds__(NT, StripGeom<R, NT>::MIN_CTAS) strip_kernel(c
             R b1 = per_len(-(G1n - G1s), rdy, idy);
             R b2 = per_len(-(s_yf2l[f1 + t] - s_yf2r[f0 + t]), rdy, idy);
             R b3 = per_len(-(s_yf3[f1 + t] * sn - s_yf3[f0 + t] * ss), rdy, idy);
-            const int cm = s4 * NT + t, c0 = s3 * NT + t, cp = s2 * NT + t;
+            const int c0 = s3 * NT + t;
             if (c.order == 2) {
-                R scx = bed_source(c, s_h[c0 - 1], s_h[c0], s_h[c0 + 1], s_z[c0 - 1], s_z[c0], s_z[c0 + 1]);
-                R scy = bed_source(c, s_h[cm], s_h[c0], s_h[cp], s_z[cm], s_z[c0], s_z[cp]);
-                a2 = a2 + per_len(scx, rdx, idx);
-                b2 = b2 + per_len(scy, rdy, idy);
+                a2 = a2 + per_len(bxc, rdx, idx);
+                b2 = b2 + per_len(by2, rdy, idy);
             }
             const R dh = a1 + b1, dhu = a2 + b3, dhv = a3 + b2;
             if (cx == 0) { xin += relu(F1w); xout += relu(-F1w); }
@@ -482,8 +473,16 @@ __global__ void __launch_bounds__(NT, StripGeom<R, NT>::MIN_CTAS) strip_kernel(c
                     gd.sf[i] = sf;
                 }
                 // ---- semi-implicit Manning friction (swe2d.py:362-370)
-                R u, v;
-                kp_velocity(c, hn, hun, hvn, u, v);
+                R u, v, ks = R(0);
+                if constexpr (sizeof(R) == 4) {
+                    // KP factor of the new depth, kept for the CFL velocity below
+                    const float h2 = hn * hn, h4 = h2 * h2;
+                    ks = hn >= c.h_dry ? 1.4142135623730951f * hn * rsqrtf(h4 + fmaxf(h4, c.kp_eps)) : 0.0f;
+                    u = hun * ks;
+                    v = hvn * ks;
+                } else {
+                    kp_velocity(c, hn, hun, hvn, u, v);
+                }
                 const R speed = dsqrt(u * u + v * v);
                 const R hf = rmax(hn, c.h_dry);
                 const R nm = cin.n;
@@ -502,7 +501,12 @@ __global__ void __launch_bounds__(NT, StripGeom<R, NT>::MIN_CTAS) strip_kernel(c
                 if (gd.ps) gd.ps[i] = rmax(gd.ps[i], wet ? dsqrt(u * u + v * v) : R(0));
                 // ---- CFL rate of the new state for the next step (swe2d.py:179-184)
                 R u2, v2;
-                kp_velocity(c, hn, hun, hvn, u2, v2);
+                if constexpr (sizeof(R) == 4) {
+                    u2 = hun * ks;
+                    v2 = hvn * ks;
+                } else {
+                    kp_velocity(c, hn, hun, hvn, u2, v2);
+                }
                 const R cw = dsqrt(c.g * hn);
                 const R rr = hn > c.h_dry ? per_len(fabs(u2) + cw, rdx, idx) + per_len(fabs(v2) + cw, rdy, idy) : R(0);
                 rate = rmax(rate, rr);
@@ -511,7 +515,9 @@ __global__ void __launch_bounds__(NT, StripGeom<R, NT>::MIN_CTAS) strip_kernel(c
                 hmax = rmax(hmax, hn);
             }
         }
-        s0 = s0 == G::RING - 1 ? 0 : s0 + 1;
+        by2 = by1;
+        by1 = by_new;
+        bxc = bx_new;
     }
     __syncthreads();
     double* out = partials + (size_t)blockIdx.x * NPART;
