@@ -27,24 +27,29 @@ struct StripRef {
     int member, x0, w, y0, y1, pad;
 };
 
+// Four values of one cell or face kept together in shared memory, so that one
+// vector access moves them: cells {h, u, v, z}, faces {F1, F2L, F2R, F3}, and the
+// x-reconstruction as {Hm, Hp, Um, Up} and {Vm, Vp, Zm, Zp} (float32: {Vm, Vp, d, sE}).
+template <class R>
+struct alignas(4 * sizeof(R)) Q4 {
+    R a, b, c, d;
+};
+
 // Shared-memory layout of one CTA
 template <class R, int NT>
 struct StripGeom {
     static constexpr int RING = 4;                 // cell rows kept (rows r-3 .. r are live)
     static constexpr int FR = 4;                   // y-face and theta rows kept (3 live)
     static constexpr int FRX = 2;                  // x-face rows kept (2 live)
-    static constexpr int NREC = 8;                 // x-reconstruction values per cell
     static constexpr int NRED = 11;                // reduced values (the reduction reuses the cell ring)
-    static constexpr size_t cells = (size_t)RING * NT * 4;
-    static constexpr size_t xrec = (size_t)NREC * NT;
-    static constexpr size_t xf = (size_t)FRX * NT * 4;
-    static constexpr size_t yf = (size_t)FR * NT * 4;
+    static constexpr size_t quads = (size_t)(RING + 2 + FRX + FR) * NT;
     static constexpr size_t th = (size_t)FR * NT;
-    static_assert(cells >= (size_t)32 * NRED, "reduction scratch must fit in the cell ring");
-    static constexpr size_t smem_bytes = sizeof(R) * (cells + xrec + xf + yf + th);
+    static_assert((size_t)4 * RING * NT >= (size_t)32 * NRED, "reduction scratch must fit in the cell ring");
+    static constexpr size_t smem_bytes = sizeof(Q4<R>) * quads + sizeof(R) * th;
     // resident CTAs per SM the float32 kernels are register-capped for (shared memory
-    // allows 14 of 64 threads); float64 keeps the compiler's choice
-    static constexpr int MIN_CTAS = sizeof(R) == 4 ? 896 / NT : 1;
+    // allows 14 of 64 threads): stage 1 at 14, the larger stage-2 body at 12 so that it
+    // keeps its live values in registers; float64 keeps the compiler's choice
+    static constexpr int min_ctas(int stage) { return sizeof(R) == 4 ? (stage == 1 ? 896 : 768) / NT : 1; }
 };
 
 // Centred bed source of one cell along one axis (swe2d.py:220), from the cell's own
@@ -205,32 +210,27 @@ __device__ __forceinline__ void block_reduce_store(T (&v)[NV], const bool* is_ma
     }
 }
 
-// x-reconstruction of one cell in shared memory (8 values); the float32 form's cell
-// depth and bed are read back from the cell ring (hrow, zrow: the cell's row there).
+// x-reconstruction of one cell in shared memory (two records at xr[t] and xr[NT + t]);
+// the float32 form's cell depth and bed come from the cell record (h0, z).
 template <class R>
-__device__ __forceinline__ void store_recon(R* xr, int stride, int t, const Recon<R>& r) {
-    xr[0 * stride + t] = r.Hm; xr[1 * stride + t] = r.Hp;
-    xr[2 * stride + t] = r.Um; xr[3 * stride + t] = r.Up;
-    xr[4 * stride + t] = r.Vm; xr[5 * stride + t] = r.Vp;
-    if constexpr (sizeof(R) == 8) {
-        xr[6 * stride + t] = r.Zm; xr[7 * stride + t] = r.Zp;
-    } else {
-        xr[6 * stride + t] = r.d; xr[7 * stride + t] = r.sE;
-    }
+__device__ __forceinline__ void store_recon(Q4<R>* xr, int t, int nt, const Recon<R>& r) {
+    xr[t] = Q4<R>{r.Hm, r.Hp, r.Um, r.Up};
+    if constexpr (sizeof(R) == 8) xr[nt + t] = Q4<R>{r.Vm, r.Vp, r.Zm, r.Zp};
+    else xr[nt + t] = Q4<R>{r.Vm, r.Vp, r.d, r.sE};
 }
 
 template <class R>
-__device__ __forceinline__ Recon<R> load_recon(const R* xr, int stride, int t, const R* hrow, const R* zrow) {
+__device__ __forceinline__ Recon<R> load_recon(const Q4<R>* xr, int t, int nt, R h0, R z) {
+    const Q4<R> p = xr[t], q = xr[nt + t];
     Recon<R> r;
-    r.Hm = xr[0 * stride + t]; r.Hp = xr[1 * stride + t];
-    r.Um = xr[2 * stride + t]; r.Up = xr[3 * stride + t];
-    r.Vm = xr[4 * stride + t]; r.Vp = xr[5 * stride + t];
+    r.Hm = p.a; r.Hp = p.b; r.Um = p.c; r.Up = p.d;
+    r.Vm = q.a; r.Vp = q.b;
     if constexpr (sizeof(R) == 8) {
-        r.Zm = xr[6 * stride + t]; r.Zp = xr[7 * stride + t];
+        r.Zm = q.c; r.Zp = q.d;
         r.z = r.d = r.h0 = r.sE = R(0);
     } else {
-        r.d = xr[6 * stride + t]; r.sE = xr[7 * stride + t];
-        r.z = zrow[t]; r.h0 = hrow[t];
+        r.d = q.c; r.sE = q.d;
+        r.z = z; r.h0 = h0;
         r.Zm = r.Zp = R(0);
     }
     return r;
@@ -242,27 +242,18 @@ __device__ __forceinline__ Recon<R> load_recon(const R* xr, int stride, int t, c
 // to the stage buffers and stage_copy_kernel moves it back (no CTA overwrites cells
 // that another CTA may still read).
 template <class R, int NT, int STAGE>
-__global__ void __launch_bounds__(NT, StripGeom<R, NT>::MIN_CTAS) strip_kernel(const Grid<R>* __restrict__ grids,
+__global__ void __launch_bounds__(NT, StripGeom<R, NT>::min_ctas(STAGE)) strip_kernel(const Grid<R>* __restrict__ grids,
                                                     const StripRef* __restrict__ strips,
                                                     const StepParams* __restrict__ params, const KC<R> c,
                                                     double* __restrict__ partials) {
     using G = StripGeom<R, NT>;
-    extern __shared__ __align__(16) unsigned char smem_raw[];
-    R* s_h = reinterpret_cast<R*>(smem_raw);          // [RING][NT]
-    R* s_u = s_h + G::RING * NT;
-    R* s_v = s_u + G::RING * NT;
-    R* s_z = s_v + G::RING * NT;
-    R* s_xr = s_z + G::RING * NT;                     // [NREC][NT]
-    R* s_xf1 = s_xr + G::NREC * NT;                   // [FRX][NT] each
-    R* s_xf2l = s_xf1 + G::FRX * NT;
-    R* s_xf2r = s_xf2l + G::FRX * NT;
-    R* s_xf3 = s_xf2r + G::FRX * NT;
-    R* s_yf1 = s_xf3 + G::FRX * NT;                   // [FR][NT] each
-    R* s_yf2l = s_yf1 + G::FR * NT;
-    R* s_yf2r = s_yf2l + G::FR * NT;
-    R* s_yf3 = s_yf2r + G::FR * NT;
-    R* s_th = s_yf3 + G::FR * NT;                     // [FR][NT]
-    R* red = s_h;                                     // after the row loop
+    extern __shared__ __align__(32) unsigned char smem_raw[];
+    Q4<R>* s_cell = reinterpret_cast<Q4<R>*>(smem_raw);   // [RING][NT] {h, u, v, z}
+    Q4<R>* s_xr = s_cell + G::RING * NT;                  // [2][NT] x-reconstruction
+    Q4<R>* s_xf = s_xr + 2 * NT;                          // [FRX][NT] x-faces {F1, F2L, F2R, F3}
+    Q4<R>* s_yf = s_xf + G::FRX * NT;                     // [FR][NT] y-faces
+    R* s_th = reinterpret_cast<R*>(s_yf + G::FR * NT);    // [FR][NT] theta
+    R* red = reinterpret_cast<R*>(smem_raw);              // after the row loop
     __shared__ R bcv[4];
     // the member's record, staged once: its field pointers are re-read every row, and
     // from global memory those reads stall the row loop
@@ -304,6 +295,7 @@ __global__ void __launch_bounds__(NT, StripGeom<R, NT>::MIN_CTAS) strip_kernel(c
     Recon<R> ylow;                                   // y-reconstruction of row r-2 (carried)
     R by1 = R(0), by2 = R(0);                        // y bed terms of rows r-2 and r-3
     R bxc = R(0);                                    // x bed term of row r-3
+    R h_r3 = R(0);                                   // depth of this column in row r-3
     // software pipeline: halo rows are fetched two rows ahead, update inputs at the start
     // of the iteration that uses them
     HaloRaw<R> ra = halo_fetch(c, gd, H, HU, HV, cx, y0 - 3);
@@ -324,37 +316,35 @@ __global__ void __launch_bounds__(NT, StripGeom<R, NT>::MIN_CTAS) strip_kernel(c
         {
             R hh, uu, vv, zz;
             halo_build(c, gd, bcv, ra, cx, r, hh, uu, vv, zz);
-            s_h[sl * NT + t] = hh; s_u[sl * NT + t] = uu; s_v[sl * NT + t] = vv; s_z[sl * NT + t] = zz;
+            s_cell[sl * NT + t] = Q4<R>{hh, uu, vv, zz};
         }
         ra = rb;
         rb = rnext;
         __syncthreads();
         // ---- P2: y-face between rows r-2 and r-1 (face index r-1), x-reconstruction of row r-2
         R by_new = R(0), bx_new = R(0);
+        Q4<R> cm2{};                                 // cell (row r-2, this column)
         if (r >= y0 - 1) {
-            const int a = s2, b = s1, cslot = s0;
+            cm2 = s_cell[s2 * NT + t];
             if (do_yface) {
                 // y-reconstruction of row r-1: normal v, tangential u
-                Recon<R> yup = reconstruct(c, s_h[a * NT + t], s_h[b * NT + t], s_h[cslot * NT + t],
-                                           s_v[a * NT + t], s_v[b * NT + t], s_v[cslot * NT + t],
-                                           s_u[a * NT + t], s_u[b * NT + t], s_u[cslot * NT + t],
-                                           s_z[a * NT + t], s_z[b * NT + t], s_z[cslot * NT + t]);
+                const Q4<R> cb = s_cell[s1 * NT + t], cc = s_cell[s0 * NT + t];
+                Recon<R> yup = reconstruct(c, cm2.a, cb.a, cc.a, cm2.c, cb.c, cc.c, cm2.b, cb.b, cc.b,
+                                           cm2.d, cb.d, cc.d);
                 const int fy = r - 1;
                 if (r >= y0 && fy >= y0 - 1 && fy <= y1 + 1) {
                     R F1 = R(0), F2L = R(0), F2R = R(0), F3 = R(0);
                     if (fy >= 0 && fy <= ny) face_flux(c, ylow, yup, F1, F2L, F2R, F3);
-                    const int fs = (fy & (G::FR - 1)) * NT + t;
-                    s_yf1[fs] = F1; s_yf2l[fs] = F2L; s_yf2r[fs] = F2R; s_yf3[fs] = F3;
+                    s_yf[(fy & (G::FR - 1)) * NT + t] = Q4<R>{F1, F2L, F2R, F3};
                 }
                 ylow = yup;
                 if (c.order == 2) by_new = bed_term(c, yup);
             }
             if (r >= y0 + 1 && do_xrec) {
-                const int rr = s2 * NT;
-                Recon<R> xr = reconstruct(c, s_h[rr + t - 1], s_h[rr + t], s_h[rr + t + 1], s_u[rr + t - 1],
-                                          s_u[rr + t], s_u[rr + t + 1], s_v[rr + t - 1], s_v[rr + t],
-                                          s_v[rr + t + 1], s_z[rr + t - 1], s_z[rr + t], s_z[rr + t + 1]);
-                store_recon(s_xr, NT, t, xr);
+                const Q4<R> cl = s_cell[s2 * NT + t - 1], cr = s_cell[s2 * NT + t + 1];
+                Recon<R> xr = reconstruct(c, cl.a, cm2.a, cr.a, cl.b, cm2.b, cr.b, cl.c, cm2.c, cr.c,
+                                          cl.d, cm2.d, cr.d);
+                store_recon(s_xr, t, NT, xr);
                 if (c.order == 2) bx_new = bed_term(c, xr);
             }
         }
@@ -363,13 +353,11 @@ __global__ void __launch_bounds__(NT, StripGeom<R, NT>::MIN_CTAS) strip_kernel(c
             const int row = r - 2;
             // ---- P3: x-faces of row r-2 (face cx between columns cx-1 and cx)
             if (do_xface && (unsigned)row < (unsigned)ny) {
-                const R* hrow = s_h + s2 * NT;
-                const R* zrow = s_z + s2 * NT;
-                Recon<R> L = load_recon(s_xr, NT, t - 1, hrow, zrow), Rr = load_recon(s_xr, NT, t, hrow, zrow);
+                const Q4<R> cl = s_cell[s2 * NT + t - 1];
+                Recon<R> L = load_recon(s_xr, t - 1, NT, cl.a, cl.d), Rr = load_recon(s_xr, t, NT, cm2.a, cm2.d);
                 R F1, F2L, F2R, F3;
                 face_flux(c, L, Rr, F1, F2L, F2R, F3);
-                const int fs = (row & (G::FRX - 1)) * NT + t;
-                s_xf1[fs] = F1; s_xf2l[fs] = F2L; s_xf2r[fs] = F2R; s_xf3[fs] = F3;
+                s_xf[(row & (G::FRX - 1)) * NT + t] = Q4<R>{F1, F2L, F2R, F3};
             }
             __syncthreads();
             // ---- P4: theta of row r-2
@@ -377,11 +365,11 @@ __global__ void __launch_bounds__(NT, StripGeom<R, NT>::MIN_CTAS) strip_kernel(c
                 R th = R(1);
                 if ((unsigned)row < (unsigned)ny && col_in) {
                     const int fr = (row & (G::FR - 1)) * NT, frx = (row & (G::FRX - 1)) * NT;
-                    const R Fw = s_xf1[frx + t], Fe = s_xf1[frx + t + 1];
-                    const R Gs = s_yf1[fr + t], Gn = s_yf1[((row + 1) & (G::FR - 1)) * NT + t];
+                    const R Fw = s_xf[frx + t].a, Fe = s_xf[frx + t + 1].a;
+                    const R Gs = s_yf[fr + t].a, Gn = s_yf[((row + 1) & (G::FR - 1)) * NT + t].a;
                     const R out = per_len(relu(Fe) + relu(-Fw), rdx, idx) + per_len(relu(Gn) + relu(-Gs), rdy, idy);
                     const R need = out * dt;
-                    const R hh = s_h[s2 * NT + t];
+                    const R hh = cm2.a;
                     th = need > hh ? hh / (need > R(0) ? need : R(1)) : R(1);
                 }
                 s_th[(row & (G::FR - 1)) * NT + t] = th;
@@ -396,17 +384,17 @@ __global__ void __launch_bounds__(NT, StripGeom<R, NT>::MIN_CTAS) strip_kernel(c
             const int tc = f0 + t;
             const R thC = s_th[tc], thW = s_th[tc - 1], thE = s_th[tc + 1];
             const R thS = s_th[((orow - 1) & (G::FR - 1)) * NT + t], thN = s_th[f1 + t];
-            const R Fw = s_xf1[fx + t], Fe = s_xf1[fx + t + 1], Gs = s_yf1[f0 + t], Gn = s_yf1[f1 + t];
+            const Q4<R> xw = s_xf[fx + t], xe = s_xf[fx + t + 1], ys = s_yf[f0 + t], yn = s_yf[f1 + t];
+            const R Fw = xw.a, Fe = xe.a, Gs = ys.a, Gn = yn.a;
             const R sw = Fw > R(0) ? thW : thC, se = Fe > R(0) ? thC : thE;
             const R ss = Gs > R(0) ? thS : thC, sn = Gn > R(0) ? thC : thN;
             const R F1w = Fw * sw, F1e = Fe * se, G1s = Gs * ss, G1n = Gn * sn;
             R a1 = per_len(-(F1e - F1w), rdx, idx);
-            R a2 = per_len(-(s_xf2l[fx + t + 1] - s_xf2r[fx + t]), rdx, idx);
-            R a3 = per_len(-(s_xf3[fx + t + 1] * se - s_xf3[fx + t] * sw), rdx, idx);
+            R a2 = per_len(-(xe.b - xw.c), rdx, idx);
+            R a3 = per_len(-(xe.d * se - xw.d * sw), rdx, idx);
             R b1 = per_len(-(G1n - G1s), rdy, idy);
-            R b2 = per_len(-(s_yf2l[f1 + t] - s_yf2r[f0 + t]), rdy, idy);
-            R b3 = per_len(-(s_yf3[f1 + t] * sn - s_yf3[f0 + t] * ss), rdy, idy);
-            const int c0 = s3 * NT + t;
+            R b2 = per_len(-(yn.b - ys.c), rdy, idy);
+            R b3 = per_len(-(yn.d * sn - ys.d * ss), rdy, idy);
             if (c.order == 2) {
                 a2 = a2 + per_len(bxc, rdx, idx);
                 b2 = b2 + per_len(by2, rdy, idy);
@@ -419,12 +407,12 @@ __global__ void __launch_bounds__(NT, StripGeom<R, NT>::MIN_CTAS) strip_kernel(c
             const size_t i = (size_t)orow * nx + cx;
             R hn, hun, hvn;
             if (STAGE == 2) {
-                const R h1 = s_h[c0];
+                const R h1 = h_r3;
                 hn = R(0.5) * (cin.h0 + h1 + dt * dh);
                 hun = R(0.5) * (cin.hu0 + cin.hu1 + dt * dhu);
                 hvn = R(0.5) * (cin.hv0 + cin.hv1 + dt * dhv);
             } else {
-                hn = s_h[c0] + dt * dh;
+                hn = h_r3 + dt * dh;
                 hun = cin.hu0 + dt * dhu;
                 hvn = cin.hv0 + dt * dhv;
             }
@@ -518,6 +506,7 @@ __global__ void __launch_bounds__(NT, StripGeom<R, NT>::MIN_CTAS) strip_kernel(c
         by2 = by1;
         by1 = by_new;
         bxc = bx_new;
+        h_r3 = cm2.a;
     }
     __syncthreads();
     double* out = partials + (size_t)blockIdx.x * NPART;
