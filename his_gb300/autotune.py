@@ -32,8 +32,9 @@ from . import _lib
 
 CANDIDATES_X = (58, 122)
 CANDIDATES_Y = (16, 24, 32, 40, 48, 64, 96, 128)
-WARMUP_STEPS = 2
-TIMED_STEPS = 3
+WARMUP_MS = 200.0        # busy the GPU before timing, so no candidate runs at ramping clocks
+TIMED_STEPS = 5          # steps per timing; each candidate keeps its best of ROUNDS timings
+ROUNDS = 3
 
 _MEM: dict[str, tuple[int, int]] = {}
 _LOCK = threading.Lock()
@@ -88,21 +89,14 @@ def candidates(shapes: list[tuple[int, int]]) -> list[tuple[int, int]]:
     return out
 
 
-def _time_candidate(lib, prec, cfgc, descs, n, tile, params, stream) -> float:
-    g = C.c_void_p()
-    _lib.check(lib.his_grid_create(prec, C.byref(cfgc), n, descs, tile[0], tile[1], C.byref(g)), "his_grid_create")
-    try:
-        for _ in range(WARMUP_STEPS):
-            _lib.check(lib.his_grid_step(g, params, None, stream.cuda_stream), "his_grid_step")
-        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-        e0.record(stream)
-        for _ in range(TIMED_STEPS):
-            _lib.check(lib.his_grid_step(g, params, None, stream.cuda_stream), "his_grid_step")
-        e1.record(stream)
-        e1.synchronize()
-        return e0.elapsed_time(e1) / TIMED_STEPS
-    finally:
-        lib.his_grid_destroy(g)
+def _time_steps(lib, g, params, stream, steps) -> float:
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    for _ in range(steps):
+        _lib.check(lib.his_grid_step(g, params, None, stream.cuda_stream), "his_grid_step")
+    e1.record(stream)
+    e1.synchronize()
+    return e0.elapsed_time(e1) / steps
 
 
 def choose_tile(device: torch.device, prec: int, cfg, descs, states: list[list[torch.Tensor]],
@@ -147,9 +141,26 @@ def choose_tile(device: torch.device, prec: int, cfg, descs, states: list[list[t
                 params[b].dt = float(min(max(dt, cfg.dt_min), cfg.dt_max))
                 params[b].t = 0.0
                 params[b].rain = 1e-5
-            times = {}
-            for tile in candidates(shapes):
-                times[f"{tile[0]}x{tile[1]}"] = _time_candidate(lib, prec, cfgc, tdesc, n, tile, params, stream)
+            cands = candidates(shapes)
+            grids = {}
+            try:
+                for tile in cands:
+                    g = C.c_void_p()
+                    _lib.check(lib.his_grid_create(prec, C.byref(cfgc), n, tdesc, tile[0], tile[1], C.byref(g)),
+                               "his_grid_create")
+                    grids[tile] = g
+                # warm up on the first candidate until the clocks have settled
+                first = grids[cands[0]]
+                per = _time_steps(lib, first, params, stream, 1)
+                _time_steps(lib, first, params, stream, max(1, int(WARMUP_MS / max(per, 1e-3))))
+                best = {tile: float("inf") for tile in cands}
+                for _ in range(ROUNDS):                      # interleaved rounds, best per candidate
+                    for tile in cands:
+                        best[tile] = min(best[tile], _time_steps(lib, grids[tile], params, stream, TIMED_STEPS))
+            finally:
+                for g in grids.values():
+                    lib.his_grid_destroy(g)
+            times = {f"{tx}x{ty}": ms for (tx, ty), ms in best.items()}
         del copies
         best = min(times, key=times.get)
         tile = tuple(int(v) for v in best.split("x"))
