@@ -1,8 +1,8 @@
 """Work-decomposition tuner of the 2-D stage kernels.
 
 The strip kernels split every member's grid into strips of at most ``tile_x``
-columns (a 64-thread CTA up to 58 columns, a 128-thread CTA up to 122) and chunks
-of at most ``tile_y`` rows (``his_grid_create``).  The fastest split depends on the
+columns (CTAs of 64, 128, 224 or 352 threads for up to 58, 122, 218 or 346
+columns) and chunks of at most ``tile_y`` rows (``his_grid_create``).  The fastest split depends on the
 grid sizes, the batch and the precision: narrow strips recompute more halo
 columns, short chunks more halo rows, and the number of strip-chunks decides how
 evenly the CTAs fill the GPU (152 SMs, 14 resident 64-thread CTAs each in float32).
@@ -30,7 +30,7 @@ import torch
 
 from . import _lib
 
-CANDIDATES_X = (58, 122)
+CANDIDATES_X = (58, 122, 218, 346)
 CANDIDATES_Y = (16, 24, 32, 40, 48, 64, 96, 128)
 WARMUP_MS = 200.0        # busy the GPU before timing, so no candidate runs at ramping clocks
 TIMED_STEPS = 5          # steps per timing; each candidate keeps its best of ROUNDS timings
@@ -71,6 +71,14 @@ def _store_file(key: str, tile: tuple[int, int], times: dict) -> None:
         pass                                   # a read-only home only loses the cache
 
 
+def strip_threads(tx: int) -> int:
+    """Threads of a strip CTA for strips of at most tx columns (3-column halo each side)."""
+    for nt in (64, 128, 224, 352):
+        if tx <= nt - 6:
+            return nt
+    raise ValueError(f"strip width {tx} above 346")
+
+
 def candidates(shapes: list[tuple[int, int]]) -> list[tuple[int, int]]:
     """Distinct decompositions: candidates that give the same strips and chunks for every
     member are timed once."""
@@ -81,7 +89,7 @@ def candidates(shapes: list[tuple[int, int]]) -> list[tuple[int, int]]:
             for ny, nx in set(shapes):
                 ns = -(-nx // tx)
                 nch = -(-ny // ty)
-                sig.append((ny, nx, -(-nx // ns), -(-ny // nch), tx <= 58))
+                sig.append((ny, nx, -(-nx // ns), -(-ny // nch), strip_threads(tx)))
             sig = tuple(sorted(sig))
             if sig not in seen:
                 seen.add(sig)

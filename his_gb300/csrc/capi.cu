@@ -19,9 +19,9 @@ int cuda_fail(cudaError_t e, const char* what) {
     return HIS_ERR_CUDA;
 }
 
-// Work decomposition of the 2-D kernels: strips of at most tx columns (a CTA of 64
-// threads up to 58 columns, 128 up to 122), chunks of ty rows.
-bool tile_supported(int tx, int ty) { return tx >= 1 && tx <= 122 && ty >= 1 && ty <= 1 << 20; }
+// Work decomposition of the 2-D kernels: strips of at most tx columns (CTAs of 64,
+// 128, 224 or 352 threads, see strip_threads), chunks of ty rows.
+bool tile_supported(int tx, int ty) { return tx >= 1 && strip_threads(tx) > 0 && ty >= 1 && ty <= 1 << 20; }
 
 Consts to_consts(const his_solver_cfg* c) {
     Consts k{};
@@ -87,7 +87,7 @@ int32_t his_grid_create(int32_t precision, const his_solver_cfg* cfg, int32_t n_
     if (n_members <= 0 || !grids) return bad("need at least one grid member");
     if (tile_x == 0) tile_x = 58;
     if (tile_y == 0) tile_y = 48;
-    if (!tile_supported(tile_x, tile_y)) return bad("unsupported work decomposition (strip width 1..122, rows >= 1)");
+    if (!tile_supported(tile_x, tile_y)) return bad("unsupported work decomposition (strip width 1..346, rows >= 1)");
     for (int m = 0; m < n_members; ++m) {
         const his_grid_desc& d = grids[m];
         std::string who = "member " + std::to_string(m) + ": ";
@@ -106,7 +106,7 @@ int32_t his_grid_create(int32_t precision, const his_solver_cfg* cfg, int32_t n_
     g->c = to_consts(cfg);
     g->n = n_members;
     g->tx = tile_x;
-    g->nt = tile_x <= 58 ? 64 : 128;
+    g->nt = strip_threads(tile_x);
     g->ty = tile_y;
     g->desc.assign(grids, grids + n_members);
     cudaGetDevice(&g->device);

@@ -81,6 +81,11 @@ int cuda_fail(cudaError_t e, const char* what);
     } while (0)
 
 bool tile_supported(int tx, int ty);
+// Threads of a strip CTA for strips of at most tx columns (a 3-column halo each side):
+// 64 up to 58 columns, 128 up to 122, 224 up to 218, 352 up to 346; 0 beyond.
+inline int strip_threads(int tx) {
+    return tx <= 58 ? 64 : tx <= 122 ? 128 : tx <= 218 ? 224 : tx <= 346 ? 352 : 0;
+}
 int check_cfg(const his_solver_cfg* c);
 Consts to_consts(const his_solver_cfg* c);
 

@@ -9,7 +9,7 @@ int grid_reduce_f32(his_grid* g, cudaStream_t s) { return grid_reduce_impl<float
 int exchange_f32(his_links* l, const Consts& c, double dt, cudaStream_t s) { return exchange_impl<float>(l, c, dt, s); }
 size_t stage_smem_bytes(int prec, int tx, int ty) {
     (void)ty;
-    const int nt = tx <= 58 ? 64 : 128;
+    const int nt = strip_threads(tx);
     return prec == HIS_PREC_F64 ? stage_smem_impl<double>(nt) : stage_smem_impl<float>(nt);
 }
 int engine_enqueue_f32(his_engine* e, int n) { return engine_enqueue_impl<float>(e, n); }

@@ -63,6 +63,8 @@ int launch_reduce_nt(his_grid* g, cudaStream_t s) {
     do {                                                         \
         if (g->nt == 64) return FN<R, 64>(g, __VA_ARGS__);       \
         if (g->nt == 128) return FN<R, 128>(g, __VA_ARGS__);     \
+        if (g->nt == 224) return FN<R, 224>(g, __VA_ARGS__);     \
+        if (g->nt == 352) return FN<R, 352>(g, __VA_ARGS__);     \
         set_error("unsupported strip width (threads per CTA)");  \
         return HIS_ERR_BAD_ARG;                                  \
     } while (0)
@@ -74,6 +76,8 @@ int grid_init_impl(his_grid* g) {
     int rc;
     if ((rc = set_strip_attrs<R, 64>()) != HIS_OK) return rc;
     if ((rc = set_strip_attrs<R, 128>()) != HIS_OK) return rc;
+    if ((rc = set_strip_attrs<R, 224>()) != HIS_OK) return rc;
+    if ((rc = set_strip_attrs<R, 352>()) != HIS_OK) return rc;
     const int n = g->n;
     std::vector<Grid<R>> H(n);
     std::vector<StripRef> strips;
@@ -164,6 +168,8 @@ template <class R>
 size_t stage_smem_impl(int nt) {
     if (nt == 64) return StripGeom<R, 64>::smem_bytes;
     if (nt == 128) return StripGeom<R, 128>::smem_bytes;
+    if (nt == 224) return StripGeom<R, 224>::smem_bytes;
+    if (nt == 352) return StripGeom<R, 352>::smem_bytes;
     return 0;
 }
 

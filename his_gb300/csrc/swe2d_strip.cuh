@@ -47,9 +47,12 @@ struct StripGeom {
     static_assert((size_t)4 * RING * NT >= (size_t)32 * NRED, "reduction scratch must fit in the cell ring");
     static constexpr size_t smem_bytes = sizeof(Q4<R>) * quads + sizeof(R) * th;
     // resident CTAs per SM the float32 kernels are register-capped for (shared memory
-    // allows 14 of 64 threads): stage 1 at 14, the larger stage-2 body at 12 so that it
-    // keeps its live values in registers; float64 keeps the compiler's choice
-    static constexpr int min_ctas(int stage) { return sizeof(R) == 4 ? (stage == 1 ? 896 : 768) / NT : 1; }
+    // allows 14 of 64 threads): about 896 threads' worth for stage 1 and 768 for the
+    // larger stage-2 body, so that it keeps its live values in registers; float64 keeps
+    // the compiler's choice (one CTA of any width must fit the register file)
+    static constexpr int min_ctas(int stage) {
+        return sizeof(R) == 4 ? ((stage == 1 ? 896 : 768) / NT > 0 ? (stage == 1 ? 896 : 768) / NT : 1) : 1;
+    }
 };
 
 // Centred bed source of one cell along one axis (swe2d.py:220), from the cell's own

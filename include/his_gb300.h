@@ -79,7 +79,7 @@ int32_t his_version(void);
 const char* his_last_error(void);
 
 /* Create a set of n_members 2-D grids computed in `precision`.  The stencil kernels
- * march up strips of at most tile_x columns (1..122) in chunks of tile_y rows
+ * march up strips of at most tile_x columns (1..346) in chunks of tile_y rows
  * (0, 0 = defaults 58 x 48); the set allocates its own stage scratch.
  * Replaces hydrointel/solver/swe2d.py:113-146 (SWE2D constructor, batched form). */
 int32_t his_grid_create(int32_t precision, const his_solver_cfg* cfg, int32_t n_members, const his_grid_desc* grids,

@@ -23,7 +23,7 @@ def _np(t):
     return t.detach().double().cpu().numpy()
 
 
-@pytest.mark.parametrize("tile", [(58, 48), (5, 3), (3, 1), (7, 2), (122, 16)])
+@pytest.mark.parametrize("tile", [(58, 48), (5, 3), (3, 1), (7, 2), (122, 16), (218, 7), (346, 5)])
 @pytest.mark.parametrize("name", list(GC.SWE2D_CASES))
 def test_swe2d_matches_oracle_and_reference(name, tile):
     sim, spec, fx = H.cuda_swe2d(name, tile=tile)

@@ -18,12 +18,13 @@ def test_candidates_are_distinct_decompositions():
         sig = []
         for ny, nx in sorted(set(shapes)):
             ns, nch = -(-nx // tx), -(-ny // ty)
-            sig.append((-(-nx // ns), -(-ny // nch), tx <= 58))
+            sig.append((-(-nx // ns), -(-ny // nch), A.strip_threads(tx)))
         sigs.add(tuple(sig))
     assert len(sigs) == len(cands)
-    # a chunk height above every grid's row count collapses to one candidate per width
+    # a chunk height above every grid's row count collapses to one candidate per CTA width
     tall = A.candidates([(10, 30)])
-    assert len(tall) == 2
+    assert len(tall) == 4
+    assert [A.strip_threads(tx) for tx in (58, 59, 122, 123, 218, 219, 346)] == [64, 128, 128, 224, 224, 352, 352]
 
 
 def test_tune_cache_round_trip(tmp_path, monkeypatch):
