@@ -63,13 +63,14 @@ class ForcingDesc(C.Structure):
                 ("q_n", C.c_int32), ("tide_base", C.c_double), ("tide_shift", C.c_double),
                 ("tide_amp", C.c_double * 4), ("tide_w", C.c_double * 4), ("tide_phase", C.c_double * 4),
                 ("q_t0", C.c_double), ("q_step", C.c_double), ("q", _F64P), ("edge_src", C.c_int32 * 4),
-                ("edge_val", C.c_double * 4)]
+                ("edge_val", C.c_double * 4), ("out_dt", C.c_double), ("n_out", C.c_int32), ("pad", C.c_int32)] + \
+               [(n, C.c_void_p) for n in ("snap_h", "snap_u", "snap_v", "snap_eta", "snap_q", "snap_t")]
 
 
 class MemberReport(C.Structure):
     _fields_ = [("t", C.c_double), ("dt_last", C.c_double), ("dt_min", C.c_double), ("dt_max", C.c_double),
                 ("rate", C.c_double), ("steps", C.c_int64), ("status", C.c_int32), ("n_sub_max", C.c_int32),
-                ("n_dt_clamped", C.c_int32), ("pad", C.c_int32), ("acc", C.c_double * 7)]
+                ("n_dt_clamped", C.c_int32), ("outputs", C.c_int32), ("acc", C.c_double * 7)]
 
 
 STATUS = {0: "running", 1: "done", 2: "non-finite state", 3: "implausible state", 4: "too many 1-D substeps"}

@@ -536,6 +536,23 @@ int32_t his_engine_create(his_grid* grid, his_net* net, his_links* links, int32_
         E.t = f.t0;
         E.dt_min = INFINITY;
         E.status = f.t_end - f.t0 > 1e-9 ? ST_RUNNING : ST_DONE;
+        if (f.n_out < 0) return bad(who + "n_out must be >= 0");
+        if (f.n_out > 0) {
+            if (!(f.out_dt > 0) || !f.snap_h || !f.snap_u || !f.snap_v || !f.snap_t)
+                return bad(who + "output needs out_dt > 0 and the snap_h, snap_u, snap_v, snap_t arrays");
+            if ((f.n_out - 1) * f.out_dt > f.t_end + 1e-9 * std::max(1.0, std::fabs(f.t_end)))
+                return bad(who + "the last output time lies beyond t_end");
+            if (net && (!f.snap_eta || !f.snap_q)) return bad(who + "output with a network needs snap_eta and snap_q");
+            E.out_dt = f.out_dt;
+            E.n_out = f.n_out;
+            E.k_out = 1;                      // slot 0 is the initial state, written by the caller
+            E.cells = grid->desc[m].ny * grid->desc[m].nx;
+            E.n1d = net ? net->h_nets[m].n_cells : 0;
+            E.snap_h = f.snap_h; E.snap_u = f.snap_u; E.snap_v = f.snap_v;
+            E.snap_eta = net ? f.snap_eta : nullptr;
+            E.snap_q = net ? f.snap_q : nullptr;
+            E.snap_t = f.snap_t;
+        }
     }
     his_engine* E = new his_engine();
     E->grid = grid; E->net = net; E->links = links; E->n = n_members; E->max_sub = max_sub;
@@ -620,7 +637,8 @@ int32_t his_engine_report(his_engine* E, his_member_report* reports, void* strea
         const EngMember& M = E->h_em[m];
         his_member_report& r = reports[m];
         r.t = M.t; r.dt_last = M.dt; r.dt_min = M.dt_min; r.dt_max = M.dt_max; r.rate = M.rate;
-        r.steps = M.steps; r.status = M.status; r.n_sub_max = M.n_sub_max; r.n_dt_clamped = M.n_clamped; r.pad = 0;
+        r.steps = M.steps; r.status = M.status; r.n_sub_max = M.n_sub_max; r.n_dt_clamped = M.n_clamped;
+        r.outputs = M.n_out > 0 ? M.k_out : 0;
         for (int j = 0; j < 7; ++j) r.acc[j] = M.acc[j];
     }
     return HIS_OK;
@@ -645,6 +663,7 @@ int32_t his_engine_resume(his_engine* E, const his_member_report* reports, const
         EngMember& M = E->h_em[m];
         M.t = r.t; M.dt = r.dt_last; M.dt_min = r.dt_min; M.dt_max = r.dt_max; M.rate = r.rate;
         M.steps = r.steps; M.status = r.status; M.n_sub_max = r.n_sub_max; M.n_clamped = r.n_dt_clamped;
+        if (M.n_out > 0) M.k_out = r.outputs < 1 ? 1 : (r.outputs > M.n_out ? M.n_out : r.outputs);
         for (int j = 0; j < 7; ++j) M.acc[j] = r.acc[j];
     }
     HIS_CK(cudaMemcpyAsync(E->d_em, E->h_em, sizeof(EngMember) * E->n, cudaMemcpyHostToDevice, E->s0));

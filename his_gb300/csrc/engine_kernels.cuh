@@ -29,7 +29,7 @@ __global__ void eng_pre_kernel(EngMember* __restrict__ em, StepParams* __restric
                                const Lnk* __restrict__ links, Consts c, double* __restrict__ netf, int max_sub,
                                double* __restrict__ exch) {
     extern __shared__ double sm[];
-    __shared__ int s_go, s_nsub;
+    __shared__ int s_go, s_nsub, s_snap;
     __shared__ double s_dt;
     const int m = blockIdx.x;
     EngMember& E = em[m];
@@ -42,7 +42,13 @@ __global__ void eng_pre_kernel(EngMember* __restrict__ em, StepParams* __restric
             if (dt < c.dt_min && s_go) E.n_clamped++;
             dt = fmin(fmax(dt, c.dt_min), c.dt_max);
         }
-        s_dt = fmin(dt, E.t_end - E.t);
+        // the step ends at the member's end or its next output time (coupling.py:255-262)
+        double limit = E.t_end;
+        const bool out_on = E.n_out > 0 && E.k_out < E.n_out;
+        const double t_next = out_on ? E.out_dt * E.k_out : 0.0;
+        if (out_on) limit = fmin(limit, t_next);
+        s_dt = fmin(dt, limit - E.t);
+        s_snap = out_on && E.t + s_dt >= t_next - 1e-9 ? E.k_out : -1;
         s_nsub = 0;
     }
     __syncthreads();
@@ -85,6 +91,13 @@ __global__ void eng_pre_kernel(EngMember* __restrict__ em, StepParams* __restric
         }
         P.active = 1;
         params_set_f32(P);
+        const int k = s_snap;
+        P.snap_k = k;
+        P.snap_h = k >= 0 ? E.snap_h + (size_t)k * E.cells : nullptr;
+        P.snap_u = k >= 0 ? E.snap_u + (size_t)k * E.cells : nullptr;
+        P.snap_v = k >= 0 ? E.snap_v + (size_t)k * E.cells : nullptr;
+        P.snap_eta = k >= 0 && E.snap_eta ? E.snap_eta + (size_t)k * E.n1d : nullptr;
+        P.snap_q = k >= 0 && E.snap_q ? E.snap_q + (size_t)k * E.n1d : nullptr;
         E.dt = dt;
         E.n_sub = s_nsub;
     }
@@ -134,6 +147,10 @@ __global__ void eng_post_kernel(EngMember* __restrict__ em, const StepParams* __
     }
     E.rate = s[P_RATE];
     E.t = E.t + E.dt;
+    if (pr.snap_k >= 0) {
+        E.snap_t[pr.snap_k] = E.t;
+        E.k_out = pr.snap_k + 1;
+    }
     E.steps += 1;
     E.dt_min = fmin(E.dt_min, E.dt);
     E.dt_max = fmax(E.dt_max, E.dt);

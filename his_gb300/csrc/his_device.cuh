@@ -48,6 +48,13 @@ struct EngMember {
     long long steps;
     int status, n_sub, n_sub_max, n_clamped;
     double acc[7];
+    // output times k * out_dt, k = 1 .. n_out - 1 (k = 0, the initial state, is written
+    // by the host); k_out is the next one.  Snapshot slots: 2-D depth and KP velocities
+    // (n_out x cells), 1-D level and discharge (n_out x n1d), and the times reached.
+    double out_dt;
+    int n_out, k_out, cells, n1d;
+    float *snap_h, *snap_u, *snap_v, *snap_eta, *snap_q;
+    double* snap_t;
 };
 
 // Piecewise-constant rain, harmonic tide and linearly interpolated inflow, as the
@@ -105,9 +112,11 @@ struct Grid {
 struct StepParams {
     double dt, t, rain;
     double bc0[4], bc1[4];
-    int active, pad;
+    int active, snap_k;              // snap_k: output slot written by this step, or -1
     float dt_f, t_f, rain_f, pad_f;
     float bc0_f[4], bc1_f[4];
+    // this step's snapshot slots (NULL: no output at the end of this step)
+    float *snap_h, *snap_u, *snap_v, *snap_eta, *snap_q;
 };
 
 __host__ __device__ inline void params_set_f32(StepParams& p) {

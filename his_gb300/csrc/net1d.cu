@@ -55,7 +55,8 @@ __global__ void net_engine_kernel(const Net* __restrict__ nets, Consts c, const 
     const int m = blockIdx.x;
     if (!params[m].active) return;
     const EngMember& E = em[m];
-    net_substeps_dev(nets[m], c, E.dt, E.n_sub, netf + (size_t)m * max_sub * 2, vol1d + m * 3, sm);
+    net_substeps_dev(nets[m], c, E.dt, E.n_sub, netf + (size_t)m * max_sub * 2, vol1d + m * 3, sm,
+                     params[m].snap_eta, params[m].snap_q);
 }
 
 int net_engine_prepare(his_engine* e) {

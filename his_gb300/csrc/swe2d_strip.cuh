@@ -258,6 +258,7 @@ __global__ void __launch_bounds__(NT, StripGeom<R, NT>::min_ctas(STAGE)) strip_k
     R* s_th = reinterpret_cast<R*>(s_yf + G::FR * NT);    // [FR][NT] theta
     R* red = reinterpret_cast<R*>(smem_raw);              // after the row loop
     __shared__ R bcv[4];
+    __shared__ float* s_snap[3];                      // output slots of this step (stage 0 / 2)
     // the member's record, staged once: its field pointers are re-read every row, and
     // from global memory those reads stall the row loop
     __shared__ __align__(16) Grid<R> s_gd;
@@ -279,6 +280,11 @@ __global__ void __launch_bounds__(NT, StripGeom<R, NT>::min_ctas(STAGE)) strip_k
     const int cx = x0 - 3 + t;                        // this thread's column
     const R dt = par_dt<R>(pr);
     if (t < 4) bcv[t] = par_bc<R>(pr, STAGE == 2, t);
+    if (t == 0) {
+        s_snap[0] = STAGE != 1 ? pr.snap_h : nullptr;
+        s_snap[1] = pr.snap_u;
+        s_snap[2] = pr.snap_v;
+    }
     const R* __restrict__ H = STAGE == 2 ? gd.h1 : gd.h;
     const R* __restrict__ HU = STAGE == 2 ? gd.hu1 : gd.hu;
     const R* __restrict__ HV = STAGE == 2 ? gd.hv1 : gd.hv;
@@ -489,7 +495,6 @@ __global__ void __launch_bounds__(NT, StripGeom<R, NT>::min_ctas(STAGE)) strip_k
                     gd.h1[i] = hn; gd.hu1[i] = hun; gd.hv1[i] = hvn;
                 }
                 if (gd.pk) gd.pk[i] = rmax(gd.pk[i], hn);
-                if (gd.ps) gd.ps[i] = rmax(gd.ps[i], wet ? dsqrt(u * u + v * v) : R(0));
                 // ---- CFL rate of the new state for the next step (swe2d.py:179-184)
                 R u2, v2;
                 if constexpr (sizeof(R) == 4) {
@@ -497,6 +502,14 @@ __global__ void __launch_bounds__(NT, StripGeom<R, NT>::min_ctas(STAGE)) strip_k
                     v2 = hvn * ks;
                 } else {
                     kp_velocity(c, hn, hun, hvn, u2, v2);
+                }
+                // running peak speed and output use the KP velocities of the new state, as the
+                // reference's snapshots do (swe2d.py:161-167, coupling.py:229-242)
+                if (gd.ps) gd.ps[i] = rmax(gd.ps[i], dsqrt(u2 * u2 + v2 * v2));
+                if (float* sh = s_snap[0]) {
+                    sh[i] = (float)hn;
+                    s_snap[1][i] = (float)u2;
+                    s_snap[2][i] = (float)v2;
                 }
                 const R cw = dsqrt(c.g * hn);
                 const R rr = hn > c.h_dry ? per_len(fabs(u2) + cw, rdx, idx) + per_len(fabs(v2) + cw, rdy, idy) : R(0);

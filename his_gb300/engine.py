@@ -18,8 +18,9 @@ its clock and accumulators exactly (``his_engine_resume``).
 from __future__ import annotations
 
 import ctypes as C
+import math
 import time
-from dataclasses import dataclass
+from dataclasses import dataclass, field
 
 import numpy as np
 import torch
@@ -49,6 +50,43 @@ class MemberResult:
     mass_error: float
 
 
+@dataclass(frozen=True)
+class FloodResult:
+    """One storm's outputs, with the fields of the reference's FloodResult
+    (hydrointel/api.py:62-82): series at the output times (float32), maxima over them,
+    infiltrated and stored volume and the mass-balance error.  extras adds the running
+    maxima over every step, the accumulated sources and the run statistics."""
+    depth_max: torch.Tensor            # (ny, nx) [m], over the output times
+    depth_series: torch.Tensor         # (nt, ny, nx) [m]
+    u: torch.Tensor                    # (nt, ny, nx) [m/s]
+    v: torch.Tensor                    # (nt, ny, nx) [m/s]
+    channel_eta: torch.Tensor          # (nt, n_nodes) [m], interior 1-D cells
+    channel_q: torch.Tensor            # (nt, n_nodes) [m^3/s]
+    times: torch.Tensor                # (nt,) [s]
+    infiltrated_volume_m3: float
+    stored_volume_m3: float
+    mass_balance_error: float
+    provenance: object = None
+    in_distribution: bool = True
+    distribution_warnings: list = field(default_factory=list)
+    extras: dict = field(default_factory=dict)
+    speed_max: torch.Tensor | None = None
+
+
+def output_count(t_end: float, interval: float) -> int:
+    """Number of output times k * interval <= t_end, k >= 0 (hydrointel/engine.py:48-50)."""
+    return int(math.floor(t_end / interval + 1e-9)) + 1
+
+
+def _level_1d(topo_z, sec, A):
+    """Channel level z + depth(A) of the trapezoid-plus-slot sections (swe1d.py:51-84)."""
+    A = np.maximum(A, 0.0)
+    b, m, yb, ts = sec["b"], sec["m"], sec["yb"], sec["ts"]
+    ab = yb * (b + m * yb)
+    y = np.where(A <= ab, 2.0 * A / (b + np.sqrt(b * b + 4.0 * m * A)), yb + (A - ab) / ts)
+    return topo_z + y
+
+
 def _report_copy(r) -> _lib.MemberReport:
     out = _lib.MemberReport()
     C.memmove(C.byref(out), C.byref(r), C.sizeof(_lib.MemberReport))
@@ -59,7 +97,7 @@ class Member:
     """One storm's device-resident state and tables, in the engine's precision."""
 
     def __init__(self, storm: Storm, dtype: torch.dtype, device: torch.device, couple: bool = True,
-                 track_peaks: bool = False, zcache: dict | None = None):
+                 track_peaks: bool = False, zcache: dict | None = None, output_interval: float | None = None):
         self.storm = storm
         self.key = storm.key
         self.dtype = dtype
@@ -92,6 +130,33 @@ class Member:
         self._forcing_arrays = (_lib.host_array(s.forcing.rain, np.float64), _lib.host_array(s.forcing.q, np.float64))
         self.record: _lib.MemberReport | None = None     # clock and accumulators to resume from
         self.volume0: float | None = None
+        self.output_interval = output_interval
+        self.n_out = 0
+        if output_interval is not None:
+            self._alloc_outputs(float(output_interval))
+
+    def _alloc_outputs(self, interval: float) -> None:
+        """Device slots for the outputs at k * interval; slot 0 is the initial state."""
+        if not interval > 0:
+            raise ValueError(f"output_interval must be positive (got {interval})")
+        n = output_count(float(self.storm.t_end), interval)
+        self.n_out = n
+        f32 = dict(dtype=torch.float32, device=self.device)
+        self.snap_h = torch.zeros((n,) + self.shape, **f32)
+        self.snap_u = torch.zeros((n,) + self.shape, **f32)
+        self.snap_v = torch.zeros((n,) + self.shape, **f32)
+        self.snap_t = torch.zeros(n, dtype=torch.float64, device=self.device)
+        self.snap_h[0] = self.h.float()                  # momentum starts at rest: u = v = 0
+        if self.coupled:
+            n1d = self.topo.n_cells
+            self.snap_eta = torch.zeros((n, n1d), **f32)
+            self.snap_q = torch.zeros((n, n1d), **f32)
+            sec = {k: self._net_arrays[k] for k in ("b", "m", "yb", "ts")}
+            eta0 = _level_1d(self._net_arrays["z"], sec, self.A.cpu().numpy())
+            self.snap_eta[0] = torch.as_tensor(eta0, dtype=torch.float32)
+            self.snap_q[0] = self.Q.float()
+        else:
+            self.snap_eta = self.snap_q = None
 
     @property
     def cells(self) -> int:
@@ -105,6 +170,8 @@ class Member:
         stage scratch and tables a grid set allocates for it."""
         ts = [self.z, self.n, self.S, self.f0, self.fc, self.k, self.h, self.hu, self.hv, self.s_filled,
               self.infil_cum, self.peak_h, self.peak_speed, self.A, self.Q]
+        if self.n_out:
+            ts += [self.snap_h, self.snap_u, self.snap_v, self.snap_t, self.snap_eta, self.snap_q]
         held = sum(t.numel() * t.element_size() for t in ts if t is not None)
         return held + 3 * self.h.numel() * self.h.element_size() + 64 * 1024
 
@@ -183,17 +250,25 @@ class Member:
         for e, kind in enumerate(s.bc):
             d.edge_src[e] = 1 if kind == "stage" else 0
             d.edge_val[e] = 0.0
+        d.n_out = self.n_out
+        if self.n_out:
+            d.out_dt = float(self.output_interval)
+            d.snap_h, d.snap_u, d.snap_v = (x.data_ptr() for x in (self.snap_h, self.snap_u, self.snap_v))
+            d.snap_t = self.snap_t.data_ptr()
+            if self.coupled:
+                d.snap_eta, d.snap_q = self.snap_eta.data_ptr(), self.snap_q.data_ptr()
 
 
 class FloodEngine:
     def __init__(self, storms: list, cfg: SolverConfig | None = None, precision: str = "fp32",
                  device=None, tile="auto", graph_steps: int = 16, max_sub: int = 64, couple: bool = True,
-                 track_peaks: bool = False):
+                 track_peaks: bool = False, output_interval: float | None = None):
         """storms: Storm objects (new members) or Member objects (members moved from
         another engine, resumed from their records).  tile: (tile_x, tile_y) strip width
         and chunk height of the 2-D kernels, (0, 0) or None for the defaults, "auto"
         (default) to let the autotuner measure the candidates for this batch (cached per
-        device, precision and batch shape)."""
+        device, precision and batch shape).  output_interval: seconds between the
+        outputs of new members (None: no series; running peaks with track_peaks)."""
         if not storms:
             raise ValueError("FloodEngine needs at least one storm")
         self.cfg = cfg or SolverConfig()
@@ -215,7 +290,7 @@ class FloodEngine:
                     raise ValueError(f"member {s.key} was built for {s.dtype} on {s.device}")
                 members.append(s)
             else:
-                members.append(Member(s, self.dtype, self.device, couple, track_peaks, zcache))
+                members.append(Member(s, self.dtype, self.device, couple, track_peaks, zcache, output_interval))
         self.members = members
         self.storms = [m.storm for m in members]
         self.B = len(members)
@@ -371,6 +446,57 @@ class FloodEngine:
                                     r.dt_max, r.n_sub_max, r.n_dt_clamped, src, v0, float(vol[b]), err))
         return out
 
+    def flood_results(self, reps=None, only: list[int] | None = None) -> list[FloodResult]:
+        """FloodResult of every member (or of the members listed in ``only``) from the
+        outputs written so far (the series ends at the last output time reached).  The
+        device data are copied to pinned host memory with non-blocking copies and one
+        synchronisation."""
+        reps = self.reports() if reps is None else reps
+        runs = self.results(reps)
+        pick = list(range(self.B)) if only is None else list(only)
+        v2 = np.zeros((self.B, 2))
+        with torch.cuda.device(self.device):
+            _lib.check(self._lib.his_grid_volumes(self._grid, _lib.as_p(v2), _lib.stream_handle()),
+                       "his_grid_volumes")
+        pending = []
+        with torch.cuda.device(self.device):
+            for b in pick:
+                m = self.members[b]
+                k = int(reps[b].outputs) if m.n_out else 0
+                host = {}
+                for name in ("snap_h", "snap_u", "snap_v", "snap_t", "snap_eta", "snap_q", "peak_h", "peak_speed"):
+                    src = getattr(m, name, None)
+                    if src is None or (name.startswith("snap") and k == 0):
+                        continue
+                    src = src[:k] if name.startswith("snap") else src
+                    dst = torch.empty(src.shape, dtype=src.dtype, pin_memory=True)
+                    dst.copy_(src, non_blocking=True)
+                    host[name] = dst
+                pending.append((k, host))
+            torch.cuda.current_stream(self.device).synchronize()
+        out = []
+        for b, (k, host) in zip(pick, pending):
+            m, run = self.members[b], runs[b]
+            h = host.get("snap_h", torch.zeros((0,) + m.shape))
+            u = host.get("snap_u", torch.zeros((0,) + m.shape))
+            v = host.get("snap_v", torch.zeros((0,) + m.shape))
+            interior = torch.as_tensor(m.topo.kind <= 1) if m.coupled else None
+            eta = host["snap_eta"][:, interior] if "snap_eta" in host else torch.zeros((len(h), 0))
+            q = host["snap_q"][:, interior] if "snap_q" in host else torch.zeros((len(h), 0))
+            extras = {"sources": run.sources, "run": run, "volume0": run.volume0, "volume": run.volume,
+                      "outputs": k}
+            if "peak_h" in host:
+                extras["depth_max_every_step"] = host["peak_h"]
+                extras["speed_max_every_step"] = host["peak_speed"]
+            out.append(FloodResult(
+                depth_max=h.amax(0) if len(h) else torch.zeros(m.shape),
+                depth_series=h, u=u, v=v, channel_eta=eta, channel_q=q,
+                times=host.get("snap_t", torch.zeros(0, dtype=torch.float64)),
+                infiltrated_volume_m3=run.sources["infiltration"], stored_volume_m3=float(v2[b, 1]),
+                mass_balance_error=run.mass_error, extras=extras,
+                speed_max=torch.sqrt(u.double() ** 2 + v.double() ** 2).amax(0).float() if len(h) else None))
+        return out
+
     def assert_mass_ok(self, tol: float | None = None) -> np.ndarray:
         tol = self.cfg.mass_tol if tol is None else tol
         res = self.results()
@@ -383,4 +509,4 @@ class FloodEngine:
         return errs
 
 
-__all__ = ["FloodEngine", "Member", "MemberResult"]
+__all__ = ["FloodEngine", "FloodResult", "Member", "MemberResult", "output_count"]

@@ -28,22 +28,28 @@ import numpy as np
 import torch
 
 from .config import SolverConfig
-from .engine import FloodEngine, Member, MemberResult
+from .engine import FloodEngine, FloodResult, Member, MemberResult, output_count
 from .swe2d import cuda_device
 from .workloads import Storm, served_requests, uneven_member
 
 
-def estimate_bytes(storm: Storm, dtype: torch.dtype, track_peaks: bool = True) -> int:
+def estimate_bytes(storm: Storm, dtype: torch.dtype, track_peaks: bool = True,
+                   output_interval: float | None = None) -> int:
     """Device bytes a storm needs as a member: 5 state planes, up to 6 field planes,
-    3 stage planes, 2 peak planes, its channel network and tables."""
+    3 stage planes, 2 peak planes, its channel network and tables, and with outputs
+    three float32 planes and two channel rows per output time."""
     planes = 5 + 2 + 3 + (3 if storm.horton is not None else 0) + (1 if storm.storage is not None else 0) + \
         (2 if track_peaks else 0)
     elem = torch.tensor([], dtype=dtype).element_size()
-    net = 0
+    net = cells1d = 0
     if storm.network is not None:
         cells1d = sum(r.n for r in storm.network.reaches) + 8 * len(storm.network.reaches)
         net = 64 * 1024 + 40 * 8 * cells1d
-    return planes * storm.cells * elem + net + 64 * 1024
+    out = 0
+    if output_interval is not None:
+        n_out = output_count(float(storm.t_end), float(output_interval))
+        out = n_out * (3 * 4 * storm.cells + 2 * 4 * cells1d + 8)
+    return planes * storm.cells * elem + net + out + 64 * 1024
 
 
 @dataclass
@@ -54,6 +60,7 @@ class Request:
     admitted: float | None = None
     finished: float | None = None
     result: MemberResult | None = None
+    flood: FloodResult | None = None
     peak_h: np.ndarray | None = None
     peak_speed: np.ndarray | None = None
     h: np.ndarray | None = None
@@ -83,10 +90,13 @@ class ServeStats:
 class FloodServer:
     def __init__(self, cfg: SolverConfig | None = None, precision: str = "fp32", device=None,
                  hbm_budget: int | None = None, max_members: int = 512, chunk_steps: int = 256,
-                 graph_steps: int = 16, tile=(58, 48), track_peaks: bool = True, keep_state: bool = False):
+                 graph_steps: int = 16, tile=(58, 48), track_peaks: bool = True, keep_state: bool = False,
+                 output_interval: float | None = None):
         """hbm_budget: device bytes the members may hold (default: 80 % of the free memory
         at start).  tile: the one work decomposition every batch uses.  keep_state:
-        copy each finished member's final depth to the host with its result."""
+        copy each finished member's final depth to the host with its result.
+        output_interval: seconds between the outputs of each request; a finished request
+        then carries a FloodResult with its series."""
         self.cfg = cfg or SolverConfig()
         self.precision = precision
         self.dtype = torch.float64 if precision == "fp64" else torch.float32
@@ -101,6 +111,7 @@ class FloodServer:
         self.tile = tuple(tile)
         self.track_peaks = track_peaks
         self.keep_state = keep_state
+        self.output_interval = output_interval
         self.queue: list[Request] = []
         self.active: list[tuple[Request, Member]] = []
         self.done: list[Request] = []
@@ -112,7 +123,7 @@ class FloodServer:
 
     # ------------------------------------------------------------ admission
     def _footprint(self, req: Request) -> int:
-        return estimate_bytes(req.storm, self.dtype, self.track_peaks)
+        return estimate_bytes(req.storm, self.dtype, self.track_peaks, self.output_interval)
 
     def _admit(self, now: float, n_active: int) -> list[tuple[Request, Member]]:
         joined = []
@@ -125,7 +136,8 @@ class FloodServer:
                                      f"({self.hbm_budget})")
                 break
             self.queue.pop(0)
-            member = Member(req.storm, self.dtype, self.device, True, self.track_peaks)
+            member = Member(req.storm, self.dtype, self.device, True, self.track_peaks,
+                            output_interval=self.output_interval)
             req.admitted = now
             self.used_bytes += need
             joined.append((req, member))
@@ -133,6 +145,10 @@ class FloodServer:
 
     def _retire(self, reps, now: float) -> list[int]:
         results = self.engine.results(reps)
+        done = [b for b in range(len(self.active)) if reps[b].status != 0]
+        floods = {}
+        if self.output_interval is not None and done:
+            floods = dict(zip(done, self.engine.flood_results(reps, only=done)))
         gone = []
         for b, (req, member) in enumerate(self.active):
             r = reps[b]
@@ -140,6 +156,7 @@ class FloodServer:
                 continue
             req.finished = now
             req.result = results[b]
+            req.flood = floods.get(b)
             if member.peak_h is not None:
                 req.peak_h = member.peak_h.cpu().numpy()
                 req.peak_speed = member.peak_speed.cpu().numpy()

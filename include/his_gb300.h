@@ -207,6 +207,18 @@ typedef struct his_forcing_desc {
     const double* q;
     int32_t edge_src[4];
     double edge_val[4];
+    /* Output (n_out = 0: none).  Output times are k * out_dt, k = 0 .. n_out - 1, each
+     * at most t_end; every step is cut short at the next output time, and the state
+     * reached there is written to slot k of DEVICE float32 arrays: snap_h, snap_u,
+     * snap_v (n_out x ny x nx: depth and KP velocities) and, with a network, snap_eta,
+     * snap_q (n_out x n_cells: level z + depth and discharge); snap_t (DEVICE float64,
+     * n_out) receives the times.  Slot 0 (the initial state) is the caller's.
+     * Replaces the output loop of hydrointel/solver/coupling.py:229-286 (snapshot,
+     * run with out_times) and the output times of hydrointel/engine.py:48-50. */
+    double out_dt;
+    int32_t n_out, pad;
+    float *snap_h, *snap_u, *snap_v, *snap_eta, *snap_q;
+    double* snap_t;
 } his_forcing_desc;
 
 /* What the host reads back per member. status: 0 running, 1 done, 2 non-finite
@@ -216,7 +228,7 @@ typedef struct his_forcing_desc {
 typedef struct his_member_report {
     double t, dt_last, dt_min, dt_max, rate;
     int64_t steps;
-    int32_t status, n_sub_max, n_dt_clamped, pad;
+    int32_t status, n_sub_max, n_dt_clamped, outputs;   /* outputs: output slots written (incl. slot 0) */
     double acc[7];
 } his_member_report;
 
