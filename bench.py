@@ -53,15 +53,27 @@ def parse():
     return p.parse_args()
 
 
-def dist_init():
+_REDUCE_DEVICE = "cuda"
+
+
+def dist_init(backend: str | None = None):
+    """One process per GPU (torchrun's RANK / LOCAL_RANK / WORLD_SIZE).  The ranks are
+    independent replicas: the only communication is the barrier and the max-over-ranks
+    of the timed region.  backend: "nccl" on GPUs (default), "gloo" for CPU tests."""
+    global _REDUCE_DEVICE
     import torch
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
     local = int(os.environ.get("LOCAL_RANK", "0"))
+    backend = backend or ("nccl" if torch.cuda.is_available() else "gloo")
+    _REDUCE_DEVICE = "cuda" if backend == "nccl" else "cpu"
     if world > 1:
         import torch.distributed as dist
-        torch.cuda.set_device(local)
-        dist.init_process_group("nccl", device_id=torch.device("cuda", local))
+        if backend == "nccl":
+            torch.cuda.set_device(local)
+            dist.init_process_group("nccl", device_id=torch.device("cuda", local))
+        else:
+            dist.init_process_group("gloo")
     elif torch.cuda.is_available():
         torch.cuda.set_device(0)
     return world, rank, local
@@ -78,9 +90,16 @@ def max_over_ranks(x: float, world: int) -> float:
         return x
     import torch
     import torch.distributed as dist
-    t = torch.tensor([x], dtype=torch.float64, device="cuda")
+    t = torch.tensor([x], dtype=torch.float64, device=_REDUCE_DEVICE)
     dist.all_reduce(t, op=dist.ReduceOp.MAX)
     return float(t.item())
+
+
+def rank_storms(members: int, rank: int):
+    """The batch a rank advances: rank 0 the named workload, every other rank its own
+    seeded storms of the same configuration (the ranks share no data)."""
+    from his_gb300 import workloads as W
+    return W.batched_uniform(members) if rank == 0 else W.batched_uniform(members, key=f"plain_full/rank{rank}")
 
 
 def peaks():
@@ -279,7 +298,7 @@ def run_ours(args, world, rank, local):
     from his_gb300.config import SolverConfig
     from his_gb300.engine import FloodEngine
     members = args.members
-    storms = W.batched_uniform(members)
+    storms = rank_storms(members, rank)
     cells = sum(s.cells for s in storms)
     tile = "auto" if args.tile == "auto" else tuple(int(v) for v in args.tile.split("x"))
     eng = FloodEngine(storms, SolverConfig(), precision="fp32", graph_steps=16, tile=tile)

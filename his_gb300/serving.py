@@ -232,6 +232,15 @@ class FloodServer:
             max_mass_error=max((r.result.mass_error for r in self.done), default=0.0), statuses=statuses)
 
 
+def shard_requests(requests: list, rank: int, world: int) -> list:
+    """The requests one of `world` independent replicas serves (round robin by arrival
+    order; the replicas share nothing, as the reference's process-per-GPU --shard i/n,
+    cli.py:190-198)."""
+    if not 0 <= rank < world:
+        raise ValueError(f"rank {rank} outside a world of {world}")
+    return list(requests[rank::world])
+
+
 def request_stream(rate_per_s: float = 2.0, horizon_s: float = 600.0, key: str = "served"):
     """The served workload: Poisson arrivals of storms drawn from the three grid sizes,
     durations U(0.5, 6) h, built ahead of time (the request payloads)."""
@@ -260,4 +269,4 @@ if __name__ == "__main__":
     main()
 
 
-__all__ = ["FloodServer", "Request", "ServeStats", "estimate_bytes", "request_stream"]
+__all__ = ["FloodServer", "Request", "ServeStats", "estimate_bytes", "request_stream", "shard_requests"]
