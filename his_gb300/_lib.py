@@ -64,7 +64,7 @@ class ForcingDesc(C.Structure):
                 ("tide_amp", C.c_double * 4), ("tide_w", C.c_double * 4), ("tide_phase", C.c_double * 4),
                 ("q_t0", C.c_double), ("q_step", C.c_double), ("q", _F64P), ("edge_src", C.c_int32 * 4),
                 ("edge_val", C.c_double * 4), ("out_dt", C.c_double), ("n_out", C.c_int32), ("pad", C.c_int32)] + \
-               [(n, C.c_void_p) for n in ("snap_h", "snap_u", "snap_v", "snap_eta", "snap_q", "snap_t")]
+               [(n, C.c_void_p) for n in ("snap_h", "snap_u", "snap_v", "snap_eta", "snap_q", "snap_t", "snap_ledger")]
 
 
 class MemberReport(C.Structure):

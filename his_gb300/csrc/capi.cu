@@ -552,6 +552,7 @@ int32_t his_engine_create(his_grid* grid, his_net* net, his_links* links, int32_
             E.snap_eta = net ? f.snap_eta : nullptr;
             E.snap_q = net ? f.snap_q : nullptr;
             E.snap_t = f.snap_t;
+            E.snap_ledger = f.snap_ledger;
         }
     }
     his_engine* E = new his_engine();

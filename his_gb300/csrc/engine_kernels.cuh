@@ -98,6 +98,7 @@ __global__ void eng_pre_kernel(EngMember* __restrict__ em, StepParams* __restric
         P.snap_v = k >= 0 ? E.snap_v + (size_t)k * E.cells : nullptr;
         P.snap_eta = k >= 0 && E.snap_eta ? E.snap_eta + (size_t)k * E.n1d : nullptr;
         P.snap_q = k >= 0 && E.snap_q ? E.snap_q + (size_t)k * E.n1d : nullptr;
+        P.snap_ledger = k >= 0 && E.snap_ledger ? E.snap_ledger + (size_t)k * LEDGER_N : nullptr;
         E.dt = dt;
         E.n_sub = s_nsub;
     }
@@ -150,6 +151,12 @@ __global__ void eng_post_kernel(EngMember* __restrict__ em, const StepParams* __
     if (pr.snap_k >= 0) {
         E.snap_t[pr.snap_k] = E.t;
         E.k_out = pr.snap_k + 1;
+        if (double* L = pr.snap_ledger) {        // the 1-D kernel writes L[L_V1D]
+            L[L_V2D] = s[P_HSUM] * gd.area;
+            L[L_STORE] = s[P_SSUM] * gd.area;
+            L[L_RAIN] = E.acc[0]; L[L_INFIL] = E.acc[1]; L[L_BND2_IN] = E.acc[2]; L[L_BND2_OUT] = E.acc[3];
+            L[L_BND1_IN] = E.acc[4]; L[L_BND1_OUT] = E.acc[5]; L[L_CLIP] = E.acc[6];
+        }
     }
     E.steps += 1;
     E.dt_min = fmin(E.dt_min, E.dt);

@@ -54,8 +54,14 @@ struct EngMember {
     double out_dt;
     int n_out, k_out, cells, n1d;
     float *snap_h, *snap_u, *snap_v, *snap_eta, *snap_q;
-    double* snap_t;
+    double *snap_t, *snap_ledger;    // ledger: LEDGER_N values per output (below)
 };
+
+// Volume ledger at an output time, in the order of the reference's snapshot ledger
+// (coupling.py:229-242): 2-D surface, 1-D channel and retained volume, then the
+// accumulated source terms.
+enum : int { L_V2D = 0, L_V1D, L_STORE, L_RAIN, L_INFIL, L_BND2_IN, L_BND2_OUT, L_BND1_IN, L_BND1_OUT, L_CLIP,
+             LEDGER_N };
 
 // Piecewise-constant rain, harmonic tide and linearly interpolated inflow, as the
 // reference evaluates them (engine.py:145-166, hyetograph.py:42-46, tide.py:29-31,
@@ -117,6 +123,7 @@ struct StepParams {
     float bc0_f[4], bc1_f[4];
     // this step's snapshot slots (NULL: no output at the end of this step)
     float *snap_h, *snap_u, *snap_v, *snap_eta, *snap_q;
+    double* snap_ledger;
 };
 
 __host__ __device__ inline void params_set_f32(StepParams& p) {

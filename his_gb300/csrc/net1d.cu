@@ -55,8 +55,9 @@ __global__ void net_engine_kernel(const Net* __restrict__ nets, Consts c, const 
     const int m = blockIdx.x;
     if (!params[m].active) return;
     const EngMember& E = em[m];
-    net_substeps_dev(nets[m], c, E.dt, E.n_sub, netf + (size_t)m * max_sub * 2, vol1d + m * 3, sm,
-                     params[m].snap_eta, params[m].snap_q);
+    const StepParams& P = params[m];
+    net_substeps_dev(nets[m], c, E.dt, E.n_sub, netf + (size_t)m * max_sub * 2, vol1d + m * 3, sm, P.snap_eta,
+                     P.snap_q, P.snap_ledger ? P.snap_ledger + L_V1D : nullptr);
 }
 
 int net_engine_prepare(his_engine* e) {

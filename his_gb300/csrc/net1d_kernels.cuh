@@ -130,7 +130,8 @@ __host__ __device__ inline size_t net_smem_bytes(int n_cells, int n_faces) {
 // bnd_out, clip summed over the substeps.  sm: net_smem_bytes() of shared memory.
 __device__ __forceinline__ void net_substeps_dev(const Net& N, const Consts& c, double dt_total, int n_sub,
                                                  const double* __restrict__ forcing, double* vols, double* sm,
-                                                 float* snap_eta = nullptr, float* snap_q = nullptr) {
+                                                 float* snap_eta = nullptr, float* snap_q = nullptr,
+                                                 double* snap_v1d = nullptr) {
     const int nc = N.n_cells, nf = N.n_faces, tid = threadIdx.x, nt = blockDim.x;
     double *A = sm, *Q = A + nc, *Ag = Q + nc, *Qg = Ag + nc, *yv = Qg + nc, *uv = yv + nc, *th = uv + nc;
     double *F1 = th + nc, *F2 = F1 + nf, *pL = F2 + nf, *pR = pL + nf, *red = pR + nf;
@@ -246,11 +247,19 @@ __device__ __forceinline__ void net_substeps_dev(const Net& N, const Consts& c, 
     }
     __syncthreads();
     for (int i = tid; i < nc; i += nt) { N.A[i] = A[i]; N.Q[i] = Q[i]; }
-    if (snap_eta)                           // output: level z + depth and discharge (coupling.py:229-242)
+    if (snap_eta) {                         // output: level z + depth and discharge (coupling.py:229-242)
+        double v1 = 0.0;
         for (int i = tid; i < nc; i += nt) {
             snap_eta[i] = (float)(N.z[i] + sec_depth(s, i, A[i]));
             snap_q[i] = (float)Q[i];
+            if (N.kind[i] <= 1) v1 += A[i] * N.dx[i];
         }
+        if (snap_v1d) {                     // channel volume over the interior cells (swe1d.py:245-247)
+            double vv[1] = {v1};
+            block_sum<1>(vv, red);
+            if (tid == 0) *snap_v1d = vv[0];
+        }
+    }
     if (tid == 0 && vols) {
         vols[0] = tot_in;
         vols[1] = tot_out;

@@ -73,6 +73,10 @@ class FloodResult:
     speed_max: torch.Tensor | None = None
 
 
+LEDGER_KEYS = ("v2d", "v1d", "storage", "rain", "infiltration", "bnd2d_in", "bnd2d_out", "bnd1d_in", "bnd1d_out",
+               "clip")
+
+
 def output_count(t_end: float, interval: float) -> int:
     """Number of output times k * interval <= t_end, k >= 0 (hydrointel/engine.py:48-50)."""
     return int(math.floor(t_end / interval + 1e-9)) + 1
@@ -146,6 +150,9 @@ class Member:
         self.snap_u = torch.zeros((n,) + self.shape, **f32)
         self.snap_v = torch.zeros((n,) + self.shape, **f32)
         self.snap_t = torch.zeros(n, dtype=torch.float64, device=self.device)
+        # volume ledger per output time (LEDGER_KEYS); slot 0 is set when the first
+        # engine measures the initial volumes
+        self.snap_ledger = torch.zeros((n, len(LEDGER_KEYS)), dtype=torch.float64, device=self.device)
         self.snap_h[0] = self.h.float()                  # momentum starts at rest: u = v = 0
         if self.coupled:
             n1d = self.topo.n_cells
@@ -171,7 +178,7 @@ class Member:
         ts = [self.z, self.n, self.S, self.f0, self.fc, self.k, self.h, self.hu, self.hv, self.s_filled,
               self.infil_cum, self.peak_h, self.peak_speed, self.A, self.Q]
         if self.n_out:
-            ts += [self.snap_h, self.snap_u, self.snap_v, self.snap_t, self.snap_eta, self.snap_q]
+            ts += [self.snap_h, self.snap_u, self.snap_v, self.snap_t, self.snap_eta, self.snap_q, self.snap_ledger]
         held = sum(t.numel() * t.element_size() for t in ts if t is not None)
         return held + 3 * self.h.numel() * self.h.element_size() + 64 * 1024
 
@@ -255,6 +262,7 @@ class Member:
             d.out_dt = float(self.output_interval)
             d.snap_h, d.snap_u, d.snap_v = (x.data_ptr() for x in (self.snap_h, self.snap_u, self.snap_v))
             d.snap_t = self.snap_t.data_ptr()
+            d.snap_ledger = self.snap_ledger.data_ptr()
             if self.coupled:
                 d.snap_eta, d.snap_q = self.snap_eta.data_ptr(), self.snap_q.data_ptr()
 
@@ -338,10 +346,19 @@ class FloodEngine:
                 _lib.check(self._lib.his_engine_resume(self._engine, reps, _lib.as_p(mask), _lib.stream_handle()),
                            "his_engine_resume")
         if any(m.volume0 is None for m in members):
-            vol = self.volumes()
+            v2 = np.zeros((self.B, 2))
+            v1 = np.zeros(self.B)
+            with torch.cuda.device(self.device):
+                _lib.check(self._lib.his_grid_volumes(self._grid, _lib.as_p(v2), _lib.stream_handle()),
+                           "his_grid_volumes")
+                if self.coupled:
+                    _lib.check(self._lib.his_net_volume(self._net, _lib.as_p(v1), _lib.stream_handle()),
+                               "his_net_volume")
             for b, m in enumerate(members):
                 if m.volume0 is None:
-                    m.volume0 = float(vol[b])
+                    m.volume0 = float(v2[b].sum() + v1[b])
+                    if m.n_out:
+                        m.snap_ledger[0, :3] = torch.tensor([v2[b, 0], v1[b], v2[b, 1]], dtype=torch.float64)
         self.n_links = [m.n_links for m in members] if self.coupled else []
 
     # ------------------------------------------------------- per-member views
@@ -464,7 +481,8 @@ class FloodEngine:
                 m = self.members[b]
                 k = int(reps[b].outputs) if m.n_out else 0
                 host = {}
-                for name in ("snap_h", "snap_u", "snap_v", "snap_t", "snap_eta", "snap_q", "peak_h", "peak_speed"):
+                for name in ("snap_h", "snap_u", "snap_v", "snap_t", "snap_eta", "snap_q", "snap_ledger", "peak_h",
+                             "peak_speed"):
                     src = getattr(m, name, None)
                     if src is None or (name.startswith("snap") and k == 0):
                         continue
@@ -485,6 +503,8 @@ class FloodEngine:
             q = host["snap_q"][:, interior] if "snap_q" in host else torch.zeros((len(h), 0))
             extras = {"sources": run.sources, "run": run, "volume0": run.volume0, "volume": run.volume,
                       "outputs": k}
+            if "snap_ledger" in host:
+                extras["ledger"] = [dict(zip(LEDGER_KEYS, row.tolist())) for row in host["snap_ledger"]]
             if "peak_h" in host:
                 extras["depth_max_every_step"] = host["peak_h"]
                 extras["speed_max_every_step"] = host["peak_speed"]

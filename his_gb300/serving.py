@@ -22,6 +22,7 @@ from __future__ import annotations
 import argparse
 import json
 import time
+from pathlib import Path
 from dataclasses import dataclass, field
 
 import numpy as np
@@ -29,6 +30,7 @@ import torch
 
 from .config import SolverConfig
 from .engine import FloodEngine, FloodResult, Member, MemberResult, output_count
+from .records import write_records
 from .swe2d import cuda_device
 from .workloads import Storm, served_requests, uneven_member
 
@@ -91,12 +93,13 @@ class FloodServer:
     def __init__(self, cfg: SolverConfig | None = None, precision: str = "fp32", device=None,
                  hbm_budget: int | None = None, max_members: int = 512, chunk_steps: int = 256,
                  graph_steps: int = 16, tile=(58, 48), track_peaks: bool = True, keep_state: bool = False,
-                 output_interval: float | None = None):
+                 output_interval: float | None = None, record_dir=None, store_factor: int = 1):
         """hbm_budget: device bytes the members may hold (default: 80 % of the free memory
         at start).  tile: the one work decomposition every batch uses.  keep_state:
         copy each finished member's final depth to the host with its result.
         output_interval: seconds between the outputs of each request; a finished request
-        then carries a FloodResult with its series."""
+        then carries a FloodResult with its series.  record_dir: with outputs, write each
+        finished request as a dataset record there (store_factor: its storage grid)."""
         self.cfg = cfg or SolverConfig()
         self.precision = precision
         self.dtype = torch.float64 if precision == "fp64" else torch.float32
@@ -112,6 +115,8 @@ class FloodServer:
         self.track_peaks = track_peaks
         self.keep_state = keep_state
         self.output_interval = output_interval
+        self.record_dir = None if record_dir is None else Path(record_dir)
+        self.store_factor = int(store_factor)
         self.queue: list[Request] = []
         self.active: list[tuple[Request, Member]] = []
         self.done: list[Request] = []
@@ -157,6 +162,8 @@ class FloodServer:
             req.finished = now
             req.result = results[b]
             req.flood = floods.get(b)
+            if req.flood is not None and self.record_dir is not None:
+                write_records([(req.storm, req.flood)], self.record_dir, self.store_factor, first_id=req.rid)
             if member.peak_h is not None:
                 req.peak_h = member.peak_h.cpu().numpy()
                 req.peak_speed = member.peak_speed.cpu().numpy()

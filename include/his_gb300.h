@@ -212,13 +212,16 @@ typedef struct his_forcing_desc {
      * reached there is written to slot k of DEVICE float32 arrays: snap_h, snap_u,
      * snap_v (n_out x ny x nx: depth and KP velocities) and, with a network, snap_eta,
      * snap_q (n_out x n_cells: level z + depth and discharge); snap_t (DEVICE float64,
-     * n_out) receives the times.  Slot 0 (the initial state) is the caller's.
+     * n_out) receives the times and snap_ledger (DEVICE float64, n_out x 10, may be NULL)
+     * the volume ledger: 2-D surface, 1-D channel and retained volume, then the
+     * accumulated rain, infiltration, bnd2d_in, bnd2d_out, bnd1d_in, bnd1d_out and clip
+     * (m^3).  Slot 0 (the initial state) is the caller's.
      * Replaces the output loop of hydrointel/solver/coupling.py:229-286 (snapshot,
      * run with out_times) and the output times of hydrointel/engine.py:48-50. */
     double out_dt;
     int32_t n_out, pad;
     float *snap_h, *snap_u, *snap_v, *snap_eta, *snap_q;
-    double* snap_t;
+    double *snap_t, *snap_ledger;
 } his_forcing_desc;
 
 /* What the host reads back per member. status: 0 running, 1 done, 2 non-finite

@@ -47,16 +47,22 @@ def test_engine_outputs_match_dropin_run():
     # float32 rounding of the snapshots)
     assert bool((res.extras["depth_max_every_step"] + 1e-6 >= res.depth_max.double()).all())
     assert res.mass_balance_error < 1e-3
+    # the volume ledger at every output time equals the drop-in run's snapshot ledger
+    for k, snap in enumerate(snaps):
+        for key, want in snap.ledger.items():
+            got = res.extras["ledger"][k][key]
+            assert got == pytest.approx(float(want), rel=1e-9, abs=1e-6), f"output {k}: ledger {key}"
     src = eng.mb.sources()
     assert res.infiltrated_volume_m3 == pytest.approx(src["infiltration"], rel=1e-9, abs=1e-6)
 
 
-def test_served_outputs_equal_solo_outputs():
+def test_served_outputs_equal_solo_outputs(tmp_path):
     from his_gb300 import workloads as W
     from his_gb300.engine import FloodEngine
     from his_gb300.serving import FloodServer
     storms = [W.uneven_member(f"serve-out/{k}", 0, (0.3 + 0.1 * k) * 3600.0) for k in range(3)]
-    srv = FloodServer(precision="fp32", chunk_steps=16, tile=(58, 48), output_interval=300.0)
+    srv = FloodServer(precision="fp32", chunk_steps=16, tile=(58, 48), output_interval=300.0,
+                      record_dir=tmp_path / "records", store_factor=2)
     st = srv.serve([(0.1 * k, s) for k, s in enumerate(storms)], max_wall_s=600)
     assert st.finished == 3 and st.rebuilds >= 2
     by_key = {r.storm.key: r for r in srv.done}
@@ -70,3 +76,15 @@ def test_served_outputs_equal_solo_outputs():
         assert torch.equal(fl.depth_series, solo.depth_series) and torch.equal(fl.u, solo.u)
         assert torch.equal(fl.channel_eta, solo.channel_eta) and torch.equal(fl.channel_q, solo.channel_q)
         assert fl.mass_balance_error == solo.mass_balance_error < 1e-3
+        assert fl.extras["ledger"] == solo.extras["ledger"]
+    # the finished requests' records, written by the server, read back
+    from his_gb300.records import load_record
+    import json
+    index = json.loads((srv.record_dir / "index.json").read_text())
+    assert len(index) == 3
+    for rid, entry in index.items():
+        rec = load_record(srv.record_dir / entry["record"])
+        req = next(r for r in srv.done if str(r.rid) == rid)
+        assert rec["meta"]["key"] == req.storm.key
+        assert rec["h"].shape == (req.flood.depth_series.shape[0], 81 // 2, 100 // 2)
+        assert torch.equal(rec["depth_max_full"], req.flood.depth_series.amax(0))
