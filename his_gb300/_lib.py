@@ -86,6 +86,8 @@ SIGNATURES = {
     "his_grid_scratch_bytes": (C.c_int64, [_H]),
     "his_grid_step": (C.c_int32, [_H, C.POINTER(StepParams), _F64P, C.c_void_p]),
     "his_grid_max_rate": (C.c_int32, [_H, _F64P, C.c_void_p]),
+    "his_grid_step_async": (C.c_int32, [_H, C.POINTER(StepParams), C.c_void_p, C.c_void_p]),
+    "his_grid_max_rate_async": (C.c_int32, [_H, C.c_void_p, C.c_void_p]),
     "his_grid_volumes": (C.c_int32, [_H, _F64P, C.c_void_p]),
     "his_grid_step_noalloc": (C.c_int32, [C.c_int32, C.POINTER(SolverCfg), C.POINTER(GridDesc),
                                           C.POINTER(StepParams), _F64P, C.c_void_p]),
@@ -93,10 +95,13 @@ SIGNATURES = {
     "his_net_destroy": (C.c_int32, [_H]),
     "his_net_step": (C.c_int32, [_H, C.c_double, C.c_int32, _F64P, _F64P, C.c_void_p]),
     "his_net_max_rate": (C.c_int32, [_H, _F64P, _I32P, C.c_void_p]),
+    "his_net_step_async": (C.c_int32, [_H, C.c_double, C.c_int32, _F64P, C.c_void_p, C.c_void_p]),
+    "his_net_max_rate_async": (C.c_int32, [_H, C.c_void_p, C.c_void_p]),
     "his_net_volume": (C.c_int32, [_H, _F64P, C.c_void_p]),
     "his_links_create": (C.c_int32, [_H, _H, C.c_int32, C.POINTER(LinksDesc), C.POINTER(_H)]),
     "his_links_destroy": (C.c_int32, [_H]),
     "his_exchange": (C.c_int32, [_H, C.POINTER(SolverCfg), C.c_double, _F64P, C.c_void_p]),
+    "his_exchange_async": (C.c_int32, [_H, C.POINTER(SolverCfg), C.c_double, C.c_void_p, C.c_void_p]),
     "his_links_exchanged": (C.c_int32, [_H, _F64P, C.c_int32, C.c_void_p]),
     "his_engine_create": (C.c_int32, [_H, _H, _H, C.c_int32, C.POINTER(ForcingDesc), C.c_int32, C.c_int32,
                                       C.POINTER(_H)]),
@@ -164,6 +169,16 @@ def as_p(a: np.ndarray):
     if a.dtype == np.int64:
         return a.ctypes.data_as(_I64P)
     raise TypeError(a.dtype)
+
+
+def on_device(device):
+    """Make ``device`` (a torch.device with an index) current for a block; no switch
+    when it already is, which is the common case on the step's hot path."""
+    import contextlib
+    import torch
+    if device.index == torch.cuda.current_device():
+        return contextlib.nullcontext()
+    return torch.cuda.device(device)
 
 
 def stream_handle(device=None) -> int:

@@ -14,7 +14,7 @@ from .infiltration import Horton
 from .swe1d import SWE1D
 from .swe2d import SWE2D
 from .topology import build_topology, sections
-from .workloads import Storm, bank_links, normal_depth
+from .workloads import BatchForcing, Storm, bank_links, normal_depth
 
 
 def storm_bcs(storm: Storm) -> dict:
@@ -41,15 +41,15 @@ def build_engine_batch(storms: list[Storm], cfg: SolverConfig | None = None, dty
     if storms[0].horton is not None:
         horton = Horton(stack([s.horton[0] for s in storms]), stack([s.horton[1] for s in storms]),
                         stack([s.horton[2] for s in storms]), storms[0].horton[3])
-    fs = [s.forcing for s in storms]
-    tide = lambda t: np.array([f.tide(t) for f in fs])
+    bf = BatchForcing([s.forcing for s in storms])
+    tide = bf.tide
     bcs = {e: EdgeBC(k, tide if k == "stage" else None) for e, k in zip(("west", "east", "south", "north"),
                                                                           storms[0].bc)}
     two = SWE2D(ter.z, stack([s.manning for s in storms]), ter.dx, cfg, bcs, device=device, dtype=dtype,
                 storage=stack([s.storage for s in storms]) if storms[0].storage is not None else None,
                 horton=horton, batch=B, tile=tile)
     two.set_state(np.stack([s.h0() for s in storms]))
-    inflow = lambda t: np.array([f.inflow(t) for f in fs])
+    inflow = bf.inflow
     one = SWE1D([s.network for s in storms], cfg, device=device, inflow=inflow, stage=tide)
     levels = []
     for s in storms:
@@ -60,7 +60,7 @@ def build_engine_batch(storms: list[Storm], cfg: SolverConfig | None = None, dty
     tp0 = build_topology(storms[0].network)
     cell1d, cells2d, length = bank_links(ter, tp0)
     links = links_from_cells(one, two, cell1d, cells2d, length)
-    rain = lambda t: np.array([f.rain_rate(t) for f in fs])
+    rain = bf.rain_rate
     return CoupledEngine(two, one, cfg, rain=rain, links=links)
 
 

@@ -20,6 +20,7 @@ import torch
 
 from . import _lib
 from ._lib import NumericalInstabilityError
+from .boundaries import edge_values
 from .config import SolverConfig
 from .massbalance import MassBalance
 from .swe1d import SWE1D
@@ -62,7 +63,7 @@ class Links:
         self._handle = C.c_void_p()
         self.B = one.B
         self.n_links = n
-        with torch.cuda.device(two.device):
+        with _lib.on_device(two.device):
             _lib.check(self._lib.his_links_create(two._handle, one._handle, one.B, descs, C.byref(self._handle)),
                        "his_links_create")
         self._owners = (one, two)
@@ -72,6 +73,14 @@ class Links:
         if h is not None and h.value and _lib._LIB is not None:
             _lib._LIB.his_links_destroy(h)
             self._handle = C.c_void_p()
+
+    def cfg_struct(self, cfg: SolverConfig):
+        """his_solver_cfg for his_exchange, rebuilt only when one of the three values
+        the exchange reads (weir_cw, exchange_limit, exchange_relax) changes."""
+        key = (cfg.weir_cw, cfg.exchange_limit, cfg.exchange_relax)
+        if getattr(self, "_cfg_key", None) != key:
+            self._cfg_c, self._cfg_key = _lib.solver_cfg(cfg), key
+        return self._cfg_c
 
     def exchanged(self, reset: bool = False) -> np.ndarray:
         out = np.zeros((self.B, 2))
@@ -104,14 +113,18 @@ def links_from_cells(one: SWE1D, two: SWE2D, cell1d, cells2d, length) -> Links:
                  uniq, one, two)
 
 
-def exchange(one: SWE1D, two: SWE2D, links: Links, dt: float, cfg: SolverConfig):
-    """Move water between the models in place; per-link volumes (m^3, + = 2-D -> 1-D)."""
-    V = np.zeros((links.B, links.n_links))
-    cfgc = _lib.solver_cfg(cfg)
-    with torch.cuda.device(two.device):
-        _lib.check(links._lib.his_exchange(links._handle, C.byref(cfgc), float(dt), _lib.as_p(V),
-                                           _lib.stream_handle()), "his_exchange")
-    V = torch.as_tensor(V, dtype=torch.float64)
+def exchange(one: SWE1D, two: SWE2D, links: Links, dt: float, cfg: SolverConfig, volumes: bool = True):
+    """Move water between the models in place; per-link volumes (m^3, + = 2-D -> 1-D)
+    as a float64 device tensor, enqueued on the current stream without waiting for it
+    (coupling.py:73-124).  ``volumes=False`` skips them (the coupled step discards them)."""
+    V = torch.empty((links.B, links.n_links), dtype=torch.float64, device=two.device) if volumes else None
+    cfgc = links.cfg_struct(cfg)
+    with _lib.on_device(two.device):
+        _lib.check(links._lib.his_exchange_async(links._handle, C.byref(cfgc), float(dt),
+                                                 V.data_ptr() if V is not None and V.numel() else None,
+                                                 _lib.stream_handle()), "his_exchange_async")
+    if V is None:
+        return None
     return V if one.batch is not None else V[0]
 
 
@@ -155,6 +168,11 @@ class CoupledEngine:
         self.mb = MassBalance(two.device, self.total_volume())
         self.log = RunLog()
         self._last_dt = 0.0
+        # CFL rates of both models land in one pinned buffer: one wait per step
+        self._rates = torch.zeros(3 * two.B, dtype=torch.float64, pin_memory=True)
+        # the 1-D substeps overlap the 2-D step (disjoint state once the exchange is done)
+        self._side = torch.cuda.Stream(two.device) if one is not None else None
+        self._exchanged = torch.cuda.Event() if one is not None else None
 
     def check_plausible(self, t: float, label: str = "") -> None:
         h = self.two.h
@@ -187,20 +205,57 @@ class CoupledEngine:
         v = v.cpu()
         return v if self.batch is not None else float(v)
 
+    def _enqueue_rates(self, need2: bool, need1: bool) -> None:
+        """Both CFL reductions of the current state, into one pinned buffer."""
+        B = self.two.B
+        with _lib.on_device(self.two.device):
+            if need2:
+                self.two.rates_async(self._rates[:B])
+            if need1:
+                self.one.rates_async(self._rates[B:])
+
+    def _wait_rates(self):
+        """Largest 2-D rate and (largest 1-D rate, any wet), after one wait for the GPU."""
+        B = self.two.B
+        with _lib.on_device(self.two.device):
+            torch.cuda.current_stream().synchronize()
+        r = self._rates.numpy()
+        rw = r[B:].reshape(B, 2)
+        return float(r[:B].max()), float(rw[:, 0].max()), bool((rw[:, 1] > 0).any())
+
     def step(self, t: float, t_limit: float, dt: float | None = None, n_sub: int | None = None) -> float:
+        """One coupled step (coupling.py:205-230): CFL dt and 1-D substep count, the
+        exchange, the 2-D step and the 1-D substeps, mass terms added on the device.
+        The step waits on the GPU once, for the CFL rates; the 1-D substeps run on a
+        side stream beside the 2-D step and join before the step returns."""
         two, one = self.two, self.one
-        dt = min(two.max_dt() if dt is None else dt, t_limit - t)
+        need1 = one is not None and n_sub is None
+        wait = dt is None or need1
+        if wait:
+            self._enqueue_rates(dt is None, need1)
+        # forcing at t does not depend on dt: evaluated while the GPU reduces
+        rain_t = self.rain(t)
+        edges_t = edge_values(two.bcs, t)
+        if wait:
+            r2, r1, wet1 = self._wait_rates()
+        dt = min(two.dt_from_rate(r2) if dt is None else dt, t_limit - t)
         if one is not None:
             if n_sub is None:
-                n_sub = max(1, math.ceil(dt / one.max_dt() - 1e-9))
-            exchange(one, two, self.links, dt, self.cfg)
-        vol = two.step(dt, t, self.rain(t))
-        mb = self.mb
-        mb.add("rain", vol.rain); mb.add("infiltration", vol.infil); mb.add("clip", vol.clip)
-        mb.add("bnd2d_in", vol.bnd_in); mb.add("bnd2d_out", vol.bnd_out)
+                n_sub = max(1, math.ceil(dt / one.dt_from_rate(r1, wet1) - 1e-9))
+            exchange(one, two, self.links, dt, self.cfg, volumes=False)
+            main = torch.cuda.current_stream(two.device)
+            self._exchanged.record(main)
+        vol = two.step(dt, t, rain_t, edges_t=edges_t)
         if one is not None:
-            v1 = one.substeps(dt, t, n_sub)
-            mb.add("bnd1d_in", v1.bnd_in); mb.add("bnd1d_out", v1.bnd_out); mb.add("clip", v1.clip)
+            # after the 2-D launch, so the host prepares the substeps while it runs
+            self._side.wait_event(self._exchanged)
+            with torch.cuda.stream(self._side):
+                v1 = one.substeps(dt, t, n_sub)
+        mb = self.mb
+        mb.add_columns(vol.TERMS, vol.table)
+        if one is not None:
+            main.wait_stream(self._side)
+            mb.add_columns(v1.TERMS, v1.table)
             self.log.n_sub_max = max(self.log.n_sub_max, n_sub)
         self.log.steps += 1
         self._last_dt = dt

@@ -19,6 +19,76 @@ int cuda_fail(cudaError_t e, const char* what) {
     return HIS_ERR_CUDA;
 }
 
+void* stage_acquire(HostStage& st, size_t bytes, int* slot) {
+    cudaError_t e = cudaSuccess;
+    if (bytes > st.bytes) {
+        size_t want = (std::max(bytes, size_t(256)) + 4095) & ~size_t(4095);
+        for (int k = 0; k < HostStage::SLOTS; ++k) {
+            if (st.done[k]) cudaEventSynchronize(st.done[k]);
+            if (st.buf[k]) cudaFreeHost(st.buf[k]);
+            st.buf[k] = nullptr;
+        }
+        st.bytes = 0;
+        for (int k = 0; k < HostStage::SLOTS && e == cudaSuccess; ++k) {
+            e = cudaMallocHost(&st.buf[k], want);
+            if (e == cudaSuccess) std::memset(st.buf[k], 0, want);   // recycled pinned pages hold old data
+            if (e == cudaSuccess && !st.done[k]) e = cudaEventCreateWithFlags(&st.done[k], cudaEventDisableTiming);
+        }
+        if (e != cudaSuccess) {
+            cuda_fail(e, "pinned staging buffer");
+            return nullptr;
+        }
+        st.bytes = want;
+    }
+    int k = st.next;
+    st.next = (k + 1) % HostStage::SLOTS;
+    if ((e = cudaEventSynchronize(st.done[k])) != cudaSuccess) {
+        cuda_fail(e, "pinned staging buffer: previous copy");
+        return nullptr;
+    }
+    *slot = k;
+    return st.buf[k];
+}
+
+int stage_release(HostStage& st, int slot, cudaStream_t s) {
+    HIS_CK(cudaEventRecord(st.done[slot], s));
+    return HIS_OK;
+}
+
+void stage_free(HostStage& st) {
+    for (int k = 0; k < HostStage::SLOTS; ++k) {
+        if (st.done[k]) {
+            cudaEventSynchronize(st.done[k]);
+            cudaEventDestroy(st.done[k]);
+        }
+        if (st.buf[k]) cudaFreeHost(st.buf[k]);
+        st.done[k] = nullptr;
+        st.buf[k] = nullptr;
+    }
+    st.bytes = 0;
+}
+
+// Output of an asynchronous entry point: device memory or page-locked host memory,
+// which the GPU writes without the host waiting.  Pageable memory is refused: a copy
+// into it would wait for the stream.  *direct is set when the kernels may store to
+// the address themselves (device, managed or mapped page-locked memory); otherwise
+// the results are copied there on the stream.
+static int check_async_out(const void* p, const char* what, bool* direct) {
+    cudaPointerAttributes a{};
+    cudaError_t e = cudaPointerGetAttributes(&a, p);
+    if (e != cudaSuccess) {
+        cudaGetLastError();
+        set_error(std::string(what) + ": not a CUDA-visible address");
+        return HIS_ERR_BAD_ARG;
+    }
+    if (a.type != cudaMemoryTypeDevice && a.type != cudaMemoryTypeHost && a.type != cudaMemoryTypeManaged) {
+        set_error(std::string(what) + " must be device or page-locked host memory");
+        return HIS_ERR_BAD_ARG;
+    }
+    *direct = a.type != cudaMemoryTypeHost || a.devicePointer == p;
+    return HIS_OK;
+}
+
 // Work decomposition of the 2-D kernels: strips of at most tx columns (CTAs of 64,
 // 128, 224 or 352 threads, see strip_threads), chunks of ty rows.
 bool tile_supported(int tx, int ty) { return tx >= 1 && strip_threads(tx) > 0 && ty >= 1 && ty <= 1 << 20; }
@@ -136,6 +206,7 @@ int32_t his_grid_destroy(his_grid* g) {
     cudaFree(g->d_out);
     cudaFree(g->d_scratch);
     if (g->h_out) cudaFreeHost(g->h_out);
+    stage_free(g->params_stage);
     delete g;
     return HIS_OK;
 }
@@ -144,10 +215,13 @@ int64_t his_grid_scratch_bytes(const his_grid* g) {
     return g ? (int64_t)(g->scratch_bytes + g->table_bytes) : 0;
 }
 
-static int upload_params(his_grid* g, const his_step_params* p, cudaStream_t s) {
-    std::vector<StepParams> sp(g->n);
+// Every field is set: the snapshot pointers and slot are NULL / -1 (the drop-in step
+// writes no output series), which the kernels read to decide whether to write one.
+static int fill_params(his_grid* g, const his_step_params* p, StepParams* sp) {
     for (int m = 0; m < g->n; ++m) {
         const his_step_params& q = p[m];
+        sp[m] = StepParams{};
+        sp[m].snap_k = -1;
         if (!std::isfinite(q.dt) || !(q.dt >= 0) || !std::isfinite(q.t) || !std::isfinite(q.rain))
             return bad("member " + std::to_string(m) + ": dt, t and rain must be finite (dt >= 0)");
         sp[m].dt = q.dt; sp[m].t = q.t; sp[m].rain = q.rain;
@@ -155,9 +229,26 @@ static int upload_params(his_grid* g, const his_step_params* p, cudaStream_t s) 
         sp[m].active = 1;
         params_set_f32(sp[m]);
     }
+    return HIS_OK;
+}
+
+static int upload_params(his_grid* g, const his_step_params* p, cudaStream_t s) {
+    std::vector<StepParams> sp(g->n);
+    int rc = fill_params(g, p, sp.data());
+    if (rc) return rc;
     // pageable source: returns once the data is staged, so `sp` may go out of scope
     HIS_CK(cudaMemcpyAsync(g->d_params, sp.data(), sizeof(StepParams) * g->n, cudaMemcpyHostToDevice, s));
     return HIS_OK;
+}
+
+static int upload_params_pinned(his_grid* g, const his_step_params* p, cudaStream_t s) {
+    int slot = 0;
+    auto* sp = (StepParams*)stage_acquire(g->params_stage, sizeof(StepParams) * g->n, &slot);
+    if (!sp) return HIS_ERR_CUDA;
+    int rc = fill_params(g, p, sp);
+    if (rc) return rc;
+    HIS_CK(cudaMemcpyAsync(g->d_params, sp, sizeof(StepParams) * g->n, cudaMemcpyHostToDevice, s));
+    return stage_release(g->params_stage, slot, s);
 }
 
 static int fetch_out(his_grid* g, cudaStream_t s) {
@@ -176,6 +267,34 @@ int32_t his_grid_step(his_grid* g, const his_step_params* params, double* vols, 
     if ((rc = fetch_out(g, s))) return rc;
     for (int m = 0; m < g->n; ++m)
         for (int j = 0; j < 5; ++j) vols[m * 5 + j] = g->h_out[m * 8 + j];
+    return HIS_OK;
+}
+
+int32_t his_grid_step_async(his_grid* g, const his_step_params* params, double* vols, void* stream) {
+    if (!g || !params) return bad("grid and params are required");
+    bool direct = false;
+    int rc = vols ? check_async_out(vols, "vols", &direct) : HIS_OK;
+    if (rc) return rc;
+    cudaStream_t s = (cudaStream_t)stream;
+    if ((rc = upload_params_pinned(g, params, s))) return rc;
+    double* ext = direct ? vols : nullptr;
+    rc = g->prec == HIS_PREC_F64 ? grid_step_f64(g, s, ext) : grid_step_f32(g, s, ext);
+    if (rc || !vols || direct) return rc;
+    HIS_CK(cudaMemcpy2DAsync(vols, 5 * sizeof(double), g->d_out, 8 * sizeof(double), 5 * sizeof(double), g->n,
+                             cudaMemcpyDefault, s));
+    return HIS_OK;
+}
+
+int32_t his_grid_max_rate_async(his_grid* g, double* rate, void* stream) {
+    if (!g || !rate) return bad("grid and rate are required");
+    bool direct = false;
+    int rc = check_async_out(rate, "rate", &direct);
+    if (rc) return rc;
+    cudaStream_t s = (cudaStream_t)stream;
+    double* ext = direct ? rate : nullptr;
+    if ((rc = g->prec == HIS_PREC_F64 ? grid_reduce_f64(g, s, ext) : grid_reduce_f32(g, s, ext)) || direct) return rc;
+    HIS_CK(cudaMemcpy2DAsync(rate, sizeof(double), g->d_out + 5, 8 * sizeof(double), sizeof(double), g->n,
+                             cudaMemcpyDefault, s));
     return HIS_OK;
 }
 
@@ -308,6 +427,7 @@ int32_t his_net_destroy(his_net* N) {
     cudaFree(N->d_forcing);
     cudaFree(N->d_out);
     if (N->h_out) cudaFreeHost(N->h_out);
+    stage_free(N->forcing_stage);
     delete N;
     return HIS_OK;
 }
@@ -323,6 +443,39 @@ int32_t his_net_step(his_net* N, double dt, int32_t n_sub, const double* forcing
     HIS_CK(cudaMemcpyAsync(N->h_out, N->d_out, sizeof(double) * 3 * N->n, cudaMemcpyDeviceToHost, s));
     HIS_CK(cudaStreamSynchronize(s));
     std::memcpy(vols, N->h_out, sizeof(double) * 3 * N->n);
+    return HIS_OK;
+}
+
+int32_t his_net_step_async(his_net* N, double dt, int32_t n_sub, const double* forcing, double* vols,
+                           void* stream) {
+    if (!N || !forcing) return bad("network and forcing are required");
+    if (n_sub < 1 || n_sub > N->max_sub) return bad("n_sub must be in [1, 256]");
+    if (!std::isfinite(dt) || !(dt >= 0)) return bad("dt must be finite and >= 0");
+    bool direct = false;
+    int rc = vols ? check_async_out(vols, "vols", &direct) : HIS_OK;
+    if (rc) return rc;
+    cudaStream_t s = (cudaStream_t)stream;
+    size_t bytes = sizeof(double) * 2 * n_sub * N->n;
+    int slot = 0;
+    void* pin = stage_acquire(N->forcing_stage, bytes, &slot);
+    if (!pin) return HIS_ERR_CUDA;
+    std::memcpy(pin, forcing, bytes);
+    HIS_CK(cudaMemcpyAsync(N->d_forcing, pin, bytes, cudaMemcpyHostToDevice, s));
+    if ((rc = stage_release(N->forcing_stage, slot, s))) return rc;
+    if ((rc = net_step_launch(N, dt, n_sub, s, direct ? vols : nullptr)) || !vols || direct) return rc;
+    HIS_CK(cudaMemcpyAsync(vols, N->d_out, sizeof(double) * 3 * N->n, cudaMemcpyDefault, s));
+    return HIS_OK;
+}
+
+int32_t his_net_max_rate_async(his_net* N, double* rate_wet, void* stream) {
+    if (!N || !rate_wet) return bad("network and rate_wet are required");
+    bool direct = false;
+    int rc = check_async_out(rate_wet, "rate_wet", &direct);
+    if (rc) return rc;
+    cudaStream_t s = (cudaStream_t)stream;
+    if ((rc = net_reduce_launch(N, s, direct ? rate_wet : nullptr)) || direct) return rc;
+    HIS_CK(cudaMemcpy2DAsync(rate_wet, 2 * sizeof(double), N->d_out, 3 * sizeof(double), 2 * sizeof(double), N->n,
+                             cudaMemcpyDefault, s));
     return HIS_OK;
 }
 
@@ -463,6 +616,16 @@ int32_t his_exchange(his_links* L, const his_solver_cfg* cfg, double dt, double*
     HIS_CK(cudaMemcpyAsync(L->h_V, L->d_V, sizeof(double) * std::max(L->total_links, 1), cudaMemcpyDeviceToHost, s));
     HIS_CK(cudaStreamSynchronize(s));
     std::memcpy(V, L->h_V, sizeof(double) * L->total_links);
+    return HIS_OK;
+}
+
+int32_t his_exchange_async(his_links* L, const his_solver_cfg* cfg, double dt, double* V, void* stream) {
+    if (!L) return bad("links are required");
+    bool direct = false;
+    int rc = V ? check_async_out(V, "V", &direct) : HIS_OK;
+    if (rc) return rc;
+    if ((rc = his_exchange(L, cfg, dt, nullptr, stream)) || !V || L->total_links == 0) return rc;
+    HIS_CK(cudaMemcpyAsync(V, L->d_V, sizeof(double) * L->total_links, cudaMemcpyDefault, (cudaStream_t)stream));
     return HIS_OK;
 }
 

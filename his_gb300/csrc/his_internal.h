@@ -9,6 +9,18 @@
 #include "his_device.cuh"
 #include "net1d_kernels.cuh"
 
+// Pinned staging of host inputs for the asynchronous entry points.  A copy from
+// pageable memory may wait for the stream to drain; one from a pinned slot never does.
+// Slots rotate, and a slot is refilled only after the copy that last read it has
+// finished (its event), which a caller that synchronises once a step never waits on.
+struct HostStage {
+    static constexpr int SLOTS = 4;
+    void* buf[SLOTS] = {};
+    cudaEvent_t done[SLOTS] = {};
+    size_t bytes = 0;
+    int next = 0;
+};
+
 struct his_grid {
     int prec = 0;
     his::Consts c{};
@@ -25,6 +37,7 @@ struct his_grid {
     void* d_scratch = nullptr;               // stage buffers of every member
     size_t scratch_bytes = 0;
     size_t table_bytes = 0;
+    HostStage params_stage;                  // his_grid_step_async parameters
 };
 
 struct his_net {
@@ -39,6 +52,7 @@ struct his_net {
     double* d_out = nullptr;                 // n x 3
     double* h_out = nullptr;
     size_t smem = 0;
+    HostStage forcing_stage;                 // his_net_step_async forcing
 };
 
 struct his_links {
@@ -74,6 +88,12 @@ namespace his {
 void set_error(const std::string& msg);
 int cuda_fail(cudaError_t e, const char* what);
 
+// Pinned slot of at least `bytes` whose last copy has finished (nullptr and the
+// error set on failure); stage_release records the copy that reads it on `s`.
+void* stage_acquire(HostStage& st, size_t bytes, int* slot);
+int stage_release(HostStage& st, int slot, cudaStream_t s);
+void stage_free(HostStage& st);
+
 #define HIS_CK(call)                                          \
     do {                                                      \
         cudaError_t e_ = (call);                              \
@@ -105,10 +125,12 @@ int noalloc_step_f32(const Consts& c, const his_grid_desc& d, const his_step_par
 // precision-specific entry points (swe2d_f64.cu / swe2d_f32.cu)
 int grid_init_f64(his_grid* g);
 int grid_init_f32(his_grid* g);
-int grid_step_f64(his_grid* g, cudaStream_t s);
-int grid_step_f32(his_grid* g, cudaStream_t s);
-int grid_reduce_f64(his_grid* g, cudaStream_t s);
-int grid_reduce_f32(his_grid* g, cudaStream_t s);
+// ext: optional device-writable copy of the outputs (step: 5 volumes per member;
+// reduce: the rate per member), written by the finalize kernel itself
+int grid_step_f64(his_grid* g, cudaStream_t s, double* ext = nullptr);
+int grid_step_f32(his_grid* g, cudaStream_t s, double* ext = nullptr);
+int grid_reduce_f64(his_grid* g, cudaStream_t s, double* ext = nullptr);
+int grid_reduce_f32(his_grid* g, cudaStream_t s, double* ext = nullptr);
 int exchange_f64(his_links* l, const Consts& c, double dt, cudaStream_t s);
 int exchange_f32(his_links* l, const Consts& c, double dt, cudaStream_t s);
 size_t stage_smem_bytes(int prec, int tx, int ty);
@@ -121,8 +143,9 @@ int engine_profile_f64(his_engine* e, int n_steps, double* ms);
 int engine_profile_f32(his_engine* e, int n_steps, double* ms);
 
 // net1d.cu
-int net_step_launch(his_net* n, double dt, int n_sub, cudaStream_t s);
-int net_reduce_launch(his_net* n, cudaStream_t s);
+// vols / rate_wet: optional device-writable outputs (3 per member; rate and wet per member)
+int net_step_launch(his_net* n, double dt, int n_sub, cudaStream_t s, double* vols = nullptr);
+int net_reduce_launch(his_net* n, cudaStream_t s, double* rate_wet = nullptr);
 int net_engine_launch(his_engine* e, cudaStream_t s);
 int net_engine_prepare(his_engine* e);
 

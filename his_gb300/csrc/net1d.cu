@@ -15,7 +15,8 @@ __global__ void net_step_kernel(const Net* __restrict__ nets, Consts c, double d
 
 // 1-D CFL rate over wet interior cells, the any-wet flag and the channel volume.
 // out: 3 per member (rate, any_wet, volume).
-__global__ void net_reduce_kernel(const Net* __restrict__ nets, Consts c, double* __restrict__ out) {
+__global__ void net_reduce_kernel(const Net* __restrict__ nets, Consts c, double* __restrict__ out,
+                                  double* __restrict__ rate_wet) {
     __shared__ double red[32 * 3];
     const Net& N = nets[blockIdx.x];
     const Sec s{N.b, N.m, N.yb, N.ts};
@@ -43,6 +44,10 @@ __global__ void net_reduce_kernel(const Net* __restrict__ nets, Consts c, double
         out[blockIdx.x * 3 + 0] = r;
         out[blockIdx.x * 3 + 1] = w;
         out[blockIdx.x * 3 + 2] = v;
+        if (rate_wet) {
+            rate_wet[blockIdx.x * 2 + 0] = r;
+            rate_wet[blockIdx.x * 2 + 1] = w;
+        }
     }
 }
 
@@ -75,16 +80,16 @@ int net_engine_launch(his_engine* e, cudaStream_t s) {
     return HIS_OK;
 }
 
-int net_step_launch(his_net* n, double dt, int n_sub, cudaStream_t s) {
+int net_step_launch(his_net* n, double dt, int n_sub, cudaStream_t s, double* vols) {
     if (n->smem > 48 * 1024)
         HIS_CK(cudaFuncSetAttribute(net_step_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)n->smem));
-    net_step_kernel<<<n->n, 128, n->smem, s>>>(n->d_nets, n->c, dt, n_sub, n->d_forcing, n->d_out);
+    net_step_kernel<<<n->n, 128, n->smem, s>>>(n->d_nets, n->c, dt, n_sub, n->d_forcing, vols ? vols : n->d_out);
     HIS_CK(cudaGetLastError());
     return HIS_OK;
 }
 
-int net_reduce_launch(his_net* n, cudaStream_t s) {
-    net_reduce_kernel<<<n->n, 128, 0, s>>>(n->d_nets, n->c, n->d_out);
+int net_reduce_launch(his_net* n, cudaStream_t s, double* rate_wet) {
+    net_reduce_kernel<<<n->n, 128, 0, s>>>(n->d_nets, n->c, n->d_out, rate_wet);
     HIS_CK(cudaGetLastError());
     return HIS_OK;
 }

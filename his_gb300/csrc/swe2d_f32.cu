@@ -4,8 +4,8 @@
 
 namespace his {
 int grid_init_f32(his_grid* g) { return grid_init_impl<float>(g); }
-int grid_step_f32(his_grid* g, cudaStream_t s) { return grid_step_impl<float>(g, s); }
-int grid_reduce_f32(his_grid* g, cudaStream_t s) { return grid_reduce_impl<float>(g, s); }
+int grid_step_f32(his_grid* g, cudaStream_t s, double* ext) { return grid_step_impl<float>(g, s, ext); }
+int grid_reduce_f32(his_grid* g, cudaStream_t s, double* ext) { return grid_reduce_impl<float>(g, s, ext); }
 int exchange_f32(his_links* l, const Consts& c, double dt, cudaStream_t s) { return exchange_impl<float>(l, c, dt, s); }
 size_t stage_smem_bytes(int prec, int tx, int ty) {
     (void)ty;

@@ -40,21 +40,21 @@ int launch_stages(his_grid* g, cudaStream_t s) {
 }
 
 template <class R, int NT>
-int launch_step_nt(his_grid* g, cudaStream_t s) {
+int launch_step_nt(his_grid* g, cudaStream_t s, double* ext) {
     int rc = launch_stages<R, NT>(g, s);
     if (rc) return rc;
     finalize_kernel<R><<<g->n, 32, 0, s>>>(reinterpret_cast<const Grid<R>*>(g->d_grids), g->d_params, g->c,
-                                           g->d_partials, g->d_out, 0);
+                                           g->d_partials, g->d_out, 0, ext);
     HIS_CK(cudaGetLastError());
     return HIS_OK;
 }
 
 template <class R, int NT>
-int launch_reduce_nt(his_grid* g, cudaStream_t s) {
+int launch_reduce_nt(his_grid* g, cudaStream_t s, double* ext) {
     auto* grids = reinterpret_cast<const Grid<R>*>(g->d_grids);
     strip_reduce_kernel<R, NT><<<g->n_tiles, NT, 0, s>>>(grids, reinterpret_cast<const StripRef*>(g->d_tiles),
                                                          make_kc<R>(g->c), g->d_partials);
-    finalize_kernel<R><<<g->n, 32, 0, s>>>(grids, g->d_params, g->c, g->d_partials, g->d_out, 1);
+    finalize_kernel<R><<<g->n, 32, 0, s>>>(grids, g->d_params, g->c, g->d_partials, g->d_out, 1, ext);
     HIS_CK(cudaGetLastError());
     return HIS_OK;
 }
@@ -144,13 +144,13 @@ int grid_init_impl(his_grid* g) {
 }
 
 template <class R>
-int grid_step_impl(his_grid* g, cudaStream_t s) {
-    HIS_NT_DISPATCH(launch_step_nt, R, g, s);
+int grid_step_impl(his_grid* g, cudaStream_t s, double* ext) {
+    HIS_NT_DISPATCH(launch_step_nt, R, g, s, ext);
 }
 
 template <class R>
-int grid_reduce_impl(his_grid* g, cudaStream_t s) {
-    HIS_NT_DISPATCH(launch_reduce_nt, R, g, s);
+int grid_reduce_impl(his_grid* g, cudaStream_t s, double* ext) {
+    HIS_NT_DISPATCH(launch_reduce_nt, R, g, s, ext);
 }
 
 template <class R>
@@ -213,7 +213,7 @@ int engine_take_rate_impl(his_engine* E) {
     // kernel attributes are set here, outside any stream capture
     if (E->pre_smem > 48 * 1024)
         HIS_CK(cudaFuncSetAttribute(eng_pre_kernel<R>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)E->pre_smem));
-    int rc = grid_reduce_impl<R>(E->grid, E->s0);
+    int rc = grid_reduce_impl<R>(E->grid, E->s0, nullptr);
     if (rc) return rc;
     eng_take_rate_kernel<<<(E->n + 127) / 128, 128, 0, E->s0>>>(E->d_em, E->grid->d_out, E->n);
     HIS_CK(cudaGetLastError());
@@ -365,7 +365,7 @@ int noalloc_step_impl(const Consts& c, const his_grid_desc& d, const his_step_pa
         strip_kernel<R, NT, 0><<<L.n_strips, NT, smem, s>>>(grid, strips, params, kc, part);
         stage_copy_kernel<R, NT><<<L.n_strips, NT, 0, s>>>(grid, strips, params);
     }
-    finalize_kernel<R><<<1, 32, 0, s>>>(grid, params, c, part, out, 0);
+    finalize_kernel<R><<<1, 32, 0, s>>>(grid, params, c, part, out, 0, nullptr);
     HIS_CK(cudaGetLastError());
     return HIS_OK;
 }

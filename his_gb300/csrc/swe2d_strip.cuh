@@ -592,7 +592,8 @@ __global__ void __launch_bounds__(NT) strip_reduce_kernel(const Grid<R>* __restr
 // volume.  mode 0: after a step; mode 1: rate and volumes only.
 template <class R>
 __global__ void finalize_kernel(const Grid<R>* __restrict__ grids, const StepParams* __restrict__ params, Consts c,
-                                const double* __restrict__ partials, double* __restrict__ out, int mode) {
+                                const double* __restrict__ partials, double* __restrict__ out, int mode,
+                                double* __restrict__ ext) {
     const int m = blockIdx.x, lane = threadIdx.x;
     const Grid<R>& gd = grids[m];
     if (mode == 0 && !params[m].active) return;
@@ -611,7 +612,10 @@ __global__ void finalize_kernel(const Grid<R>* __restrict__ grids, const StepPar
     o[5] = s[P_RATE];
     o[6] = s[P_HSUM] * gd.area;
     o[7] = s[P_SSUM] * gd.area;
-    if (mode != 0) return;
+    if (mode != 0) {
+        if (ext) ext[m] = s[P_RATE];
+        return;
+    }
     const StepParams& pr = params[m];
     const double dt = (double)R(pr.dt);
     double qin = s[P_XIN1] * gd.dy + s[P_YIN1] * gd.dx;
@@ -630,6 +634,10 @@ __global__ void finalize_kernel(const Grid<R>* __restrict__ grids, const StepPar
     else o[2] = (double)(R(pr.rain) * R(pr.dt)) * ((double)((long long)gd.nx * gd.ny) * gd.area);
     o[3] = s[P_INFIL] * gd.area;
     o[4] = clip;
+    if (ext) {
+#pragma unroll
+        for (int j = 0; j < 5; ++j) ext[(size_t)m * 5 + j] = o[j];
+    }
 }
 
 }  // namespace his

@@ -48,6 +48,31 @@ class MassBalance:
             self.acc[key] = torch.zeros_like(value)
         self.acc[key] += value
 
+    def add_columns(self, names: tuple, values) -> None:
+        """Add the columns of ``values`` (B x len(names) float64 device tensor) to the
+        named terms in one device operation.  Each term receives the same float64 sums
+        as ``add`` one column at a time (every index is distinct, so each accumulator
+        element gets exactly one addition per call)."""
+        import torch
+        cache = self.__dict__.setdefault("_col_idx", {})
+        idx = cache.get((names, values.device))
+        if idx is None:
+            for n in names:
+                if n not in TERMS:
+                    raise KeyError(n)
+            if len(set(names)) != len(names):
+                raise ValueError("a term may appear once per add_columns call")
+            idx = cache[(names, values.device)] = torch.as_tensor([TERMS.index(n) for n in names],
+                                                                   device=values.device)
+        B = self.v0.size
+        if tuple(values.shape) != (B, len(names)):
+            raise ValueError(f"mass columns have shape {tuple(values.shape)}, expected ({B}, {len(names)})")
+        key = ("_columns", str(values.device))
+        acc = self.acc.get(key)
+        if acc is None:
+            acc = self.acc[key] = torch.zeros((len(TERMS), B), dtype=torch.float64, device=values.device)
+        acc.index_add_(0, idx, values.t().to(torch.float64))
+
     def set_totals(self, totals: dict) -> None:
         """Replace the accumulators by totals computed elsewhere (e.g. on the device)."""
         import torch
@@ -62,6 +87,11 @@ class MassBalance:
         zero = np.zeros(self.v0.shape)
         out = {k: zero.copy() for k in TERMS}
         for (k, _), v in self.acc.items():
+            if k == "_columns":
+                cols = _np(v)
+                for i, name in enumerate(TERMS):
+                    out[name] = out[name] + cols[i].reshape(self.v0.shape)
+                continue
             out[k] = out[k] + _np(v)
         return {k: (v if self.batch is not None else float(v)) for k, v in out.items()}
 

@@ -9,7 +9,7 @@ junctions are float64 islands of the production form).
 from __future__ import annotations
 
 import ctypes as C
-from dataclasses import dataclass
+from dataclasses import dataclass, field
 
 import numpy as np
 import torch
@@ -26,6 +26,10 @@ class Step1DVolumes:
     bnd_in: torch.Tensor
     bnd_out: torch.Tensor
     clip: torch.Tensor
+    # the three columns above as one (B, 3) device table, for one-operation accounting
+    table: torch.Tensor | None = field(default=None, repr=False, compare=False)
+
+    TERMS = ("bnd1d_in", "bnd1d_out", "clip")
 
 
 @dataclass
@@ -131,7 +135,7 @@ class SWE1D:
             d.A = self._A.data_ptr() + b * stride
             d.Q = self._Q.data_ptr() + b * stride
         cfgc = _lib.solver_cfg(cfg)
-        with torch.cuda.device(self.device):
+        with _lib.on_device(self.device):
             _lib.check(self._lib.his_net_create(C.byref(cfgc), self.B, descs, C.byref(self._handle)),
                        "his_net_create")
 
@@ -170,16 +174,27 @@ class SWE1D:
     def member_rates(self):
         rate = np.zeros(self.B)
         wet = np.zeros(self.B, dtype=np.int32)
-        with torch.cuda.device(self.device):
+        with _lib.on_device(self.device):
             _lib.check(self._lib.his_net_max_rate(self._handle, _lib.as_p(rate), _lib.as_p(wet),
                                                   _lib.stream_handle()), "his_net_max_rate")
         return rate, wet
 
+    def rates_async(self, out: torch.Tensor) -> None:
+        """Enqueue per-member (rate, wet) into ``out`` (B x 2 float64, device or pinned
+        host memory), valid once the current stream reaches this point."""
+        with _lib.on_device(self.device):
+            _lib.check(self._lib.his_net_max_rate_async(self._handle, out.data_ptr(), _lib.stream_handle()),
+                       "his_net_max_rate_async")
+
     def max_dt(self) -> float:
         rate, wet = self.member_rates()
-        if not wet.any():
+        return self.dt_from_rate(float(rate.max()), bool(wet.any()))
+
+    def dt_from_rate(self, rate: float, any_wet: bool) -> float:
+        """The 1-D CFL choice of swe1d.py:253-262 from the batch's largest rate."""
+        if not any_wet:
             return self.cfg.dt_max
-        return min(self.cfg.cfl_1d / float(rate.max()), self.cfg.dt_max)
+        return min(self.cfg.cfl_1d / rate, self.cfg.dt_max)
 
     # ----------------------------------------------------------------- step
     def forcing(self, t: float) -> np.ndarray:
@@ -193,12 +208,12 @@ class SWE1D:
         sub = dt / n_sub
         f = np.stack([self.forcing(t + k * sub) for k in range(n_sub)], axis=1)   # (B, n_sub, 2)
         f = np.ascontiguousarray(f, dtype=np.float64)
-        vols = np.zeros((self.B, 3))
-        with torch.cuda.device(self.device):
-            _lib.check(self._lib.his_net_step(self._handle, float(dt), int(n_sub), _lib.as_p(f), _lib.as_p(vols),
-                                              _lib.stream_handle()), "his_net_step")
-        cols = [torch.as_tensor(vols[:, j].copy(), dtype=torch.float64).reshape(self.bshape) for j in range(3)]
-        return Step1DVolumes(*cols)
+        vols = torch.empty((self.B, 3), dtype=torch.float64, device=self.device)
+        with _lib.on_device(self.device):
+            _lib.check(self._lib.his_net_step_async(self._handle, float(dt), int(n_sub), _lib.as_p(f),
+                                                    vols.data_ptr(), _lib.stream_handle()), "his_net_step_async")
+        cols = vols.t().unbind(0) if self.bshape else vols[0].unbind(0)
+        return Step1DVolumes(*cols, table=vols)
 
     def step(self, dt: float, t: float) -> Step1DVolumes:
         return self.substeps(dt, t, 1)

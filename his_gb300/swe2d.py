@@ -12,7 +12,7 @@ current CUDA device).
 from __future__ import annotations
 
 import ctypes as C
-from dataclasses import dataclass
+from dataclasses import dataclass, field
 
 import numpy as np
 import torch
@@ -32,6 +32,10 @@ class StepVolumes:
     rain: torch.Tensor
     infil: torch.Tensor
     clip: torch.Tensor
+    # the five columns above as one (B, 5) device table, for one-operation accounting
+    table: torch.Tensor | None = field(default=None, repr=False, compare=False)
+
+    TERMS = ("bnd2d_in", "bnd2d_out", "rain", "infiltration", "clip")
 
 
 def cuda_device(device=None) -> torch.device:
@@ -44,8 +48,13 @@ def cuda_device(device=None) -> torch.device:
     return torch.device("cuda", torch.cuda.current_device())
 
 
+_STEP_DTYPE = np.dtype(_lib.StepParams)
+
+
 def per_member(values, B: int, dtype=np.float64) -> np.ndarray:
     """1 value (broadcast) or one per member, else ValueError (swe2d.py:282-296)."""
+    if all(isinstance(v, (float, int)) for v in values):
+        return np.repeat(np.asarray(values, dtype=dtype)[:, None], B, axis=1)
     out = []
     for v in values:
         if torch.is_tensor(v):
@@ -124,7 +133,7 @@ class SWE2D:
             d.rain_weight = self._plane(self.rain_weight, b)
         tx, ty = tile if tile is not None else (0, 0)
         cfgc = _lib.solver_cfg(cfg)
-        with torch.cuda.device(self.device):
+        with _lib.on_device(self.device):
             _lib.check(self._lib.his_grid_create(self.prec, C.byref(cfgc), self.B, descs, int(tx), int(ty),
                                                  C.byref(self._handle)), "his_grid_create")
         self._descs = descs
@@ -190,14 +199,24 @@ class SWE2D:
     # -------------------------------------------------------------- time step
     def member_rates(self) -> np.ndarray:
         out = np.zeros(self.B)
-        with torch.cuda.device(self.device):
+        with _lib.on_device(self.device):
             _lib.check(self._lib.his_grid_max_rate(self._handle, _lib.as_p(out), _lib.stream_handle()),
                        "his_grid_max_rate")
         return out
 
+    def rates_async(self, out: torch.Tensor) -> None:
+        """Enqueue the per-member CFL rates into ``out`` (B float64, device or pinned
+        host memory), valid once the current stream reaches this point."""
+        with _lib.on_device(self.device):
+            _lib.check(self._lib.his_grid_max_rate_async(self._handle, out.data_ptr(), _lib.stream_handle()),
+                       "his_grid_max_rate_async")
+
     def max_dt(self) -> float:
         """CFL step over the whole batch (the reference shares one dt across members)."""
-        m = float(self.member_rates().max())
+        return self.dt_from_rate(float(self.member_rates().max()))
+
+    def dt_from_rate(self, m: float) -> float:
+        """The CFL choice of swe2d.py:186-193 from the batch's largest rate."""
         cfg = self.cfg
         dt = cfg.cfl / m if m > 0 else cfg.dt_max
         if dt < cfg.dt_min or dt > cfg.dt_max:
@@ -206,26 +225,28 @@ class SWE2D:
             dt = min(max(dt, cfg.dt_min), cfg.dt_max)
         return dt
 
-    def step_params(self, dt: float, t: float, rain_rate=0.0):
-        pm = per_member([rain_rate] + edge_values(self.bcs, t) + edge_values(self.bcs, t + dt), self.B)
-        params = (_lib.StepParams * self.B)()
-        for b in range(self.B):
-            p = params[b]
-            p.dt, p.t, p.rain = float(dt), float(t), float(pm[0, b])
-            for e in range(4):
-                p.bc_t[e] = float(pm[1 + e, b])
-                p.bc_t_dt[e] = float(pm[5 + e, b])
-        return params
+    def step_params(self, dt: float, t: float, rain_rate=0.0, edges_t=None):
+        """his_step_params of every member, as a numpy record array with the C layout
+        (filled column-wise: a Python loop over members costs more than a GPU step).
+        ``edges_t``: the edge values at t, when the caller has them already."""
+        at_t = edge_values(self.bcs, t) if edges_t is None else edges_t
+        pm = per_member([rain_rate] + at_t + edge_values(self.bcs, t + dt), self.B)
+        a = np.empty(self.B, dtype=_STEP_DTYPE)
+        a["dt"], a["t"], a["rain"] = float(dt), float(t), pm[0]
+        a["bc_t"], a["bc_t_dt"] = pm[1:5].T, pm[5:9].T
+        self._params_keep = a
+        return a.ctypes.data_as(C.POINTER(_lib.StepParams))
 
-    def step(self, dt: float, t: float, rain_rate=0.0) -> StepVolumes:
-        params = self.step_params(dt, t, rain_rate)
-        vols = np.zeros((self.B, 5))
-        with torch.cuda.device(self.device):
-            _lib.check(self._lib.his_grid_step(self._handle, params, _lib.as_p(vols), _lib.stream_handle()),
-                       "his_grid_step")
-        shape = self.bshape
-        cols = [torch.as_tensor(vols[:, j].copy(), dtype=torch.float64).reshape(shape) for j in range(5)]
-        return StepVolumes(*cols)
+    def step(self, dt: float, t: float, rain_rate=0.0, edges_t=None) -> StepVolumes:
+        """One SSP-RK2 step, enqueued on the current stream without waiting for it; the
+        volumes are float64 device tensors, as the reference's are."""
+        params = self.step_params(dt, t, rain_rate, edges_t)
+        vols = torch.empty((self.B, 5), dtype=torch.float64, device=self.device)
+        with _lib.on_device(self.device):
+            _lib.check(self._lib.his_grid_step_async(self._handle, params, vols.data_ptr(), _lib.stream_handle()),
+                       "his_grid_step_async")
+        cols = vols.t().unbind(0) if self.bshape else vols[0].unbind(0)
+        return StepVolumes(*cols, table=vols)
 
     def scratch_bytes(self) -> int:
         return int(self._lib.his_grid_scratch_bytes(self._handle))

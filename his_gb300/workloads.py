@@ -85,6 +85,67 @@ class Forcing:
         return float((1 - w) * self.q[k] + w * self.q[k + 1])
 
 
+class BatchForcing:
+    """The forcing of B storms evaluated for all members at once (arrays over the
+    members), with the arithmetic of Forcing per member: the same floor, clamp and
+    interpolation steps in float64; the tide's cosines through numpy, which may differ
+    from math.cos by an ulp."""
+
+    def __init__(self, forcings: list[Forcing]):
+        fs = list(forcings)
+        self.B = len(fs)
+        self.rain_t0 = np.array([f.rain_t0 for f in fs], np.float64)
+        self.rain_step = np.array([f.rain_step for f in fs], np.float64)
+        self.rain_n = np.array([len(f.rain) for f in fs], np.int64)
+        self.rain = _ragged([f.rain for f in fs])
+        self.tide_base = np.array([f.tide_base for f in fs], np.float64)
+        self.tide_shift = np.array([f.tide_shift for f in fs], np.float64)
+        self.tide_on = np.array([bool(f.tide_on) for f in fs])
+        nh = max((len(f.tide_amp) for f in fs), default=0)
+        pad = lambda xs: np.array([list(x) + [0.0] * (nh - len(x)) for x in xs], np.float64).reshape(self.B, nh)
+        self.tide_amp = pad([f.tide_amp for f in fs])
+        self.tide_w = pad([f.tide_w for f in fs])
+        self.tide_phase = pad([f.tide_phase for f in fs])
+        self.q_t0 = np.array([f.q_t0 for f in fs], np.float64)
+        self.q_step = np.array([f.q_step for f in fs], np.float64)
+        self.q_n = np.array([len(f.q) for f in fs], np.int64)
+        self.q = _ragged([f.q for f in fs])
+        self._rows = np.arange(self.B)
+
+    def rain_rate(self, t: float) -> np.ndarray:
+        k = np.floor((t - self.rain_t0) / self.rain_step + 1e-9).astype(np.int64)
+        ok = (k >= 0) & (k < self.rain_n)
+        return np.where(ok, self.rain[self._rows, np.clip(k, 0, max(self.rain.shape[1] - 1, 0))], 0.0) \
+            if self.rain.shape[1] else np.zeros(self.B)
+
+    def tide(self, t: float) -> np.ndarray:
+        tt = t + self.tide_shift
+        eta = np.zeros(self.B)
+        for j in range(self.tide_amp.shape[1]):      # harmonics in order, as Forcing.tide sums them
+            eta = eta + self.tide_amp[:, j] * np.cos(self.tide_w[:, j] * tt - self.tide_phase[:, j])
+        return self.tide_base + np.where(self.tide_on, eta, 0.0)
+
+    def inflow(self, t: float) -> np.ndarray:
+        if not self.q.shape[1]:
+            return np.zeros(self.B)
+        x = (t - self.q_t0) / self.q_step
+        last = np.maximum(self.q_n - 1, 0)
+        k = np.clip(x.astype(np.int64), 0, np.maximum(last - 1, 0))
+        w = x - k
+        mid = (1 - w) * self.q[self._rows, k] + w * self.q[self._rows, np.minimum(k + 1, last)]
+        out = np.where(x <= 0, self.q[:, 0], np.where(x >= last, self.q[self._rows, last], mid))
+        return np.where(self.q_n > 0, out, 0.0)
+
+
+def _ragged(rows) -> np.ndarray:
+    """Rows of different lengths as one zero-padded (B, max length) array."""
+    n = max((len(r) for r in rows), default=0)
+    out = np.zeros((len(rows), n))
+    for i, r in enumerate(rows):
+        out[i, :len(r)] = r
+    return out
+
+
 def alternating_block(duration_s: float, step_s: float, peak_mmh: float, position: float = 0.5) -> np.ndarray:
     """Alternating-block hyetograph from a generic IDF depth curve D(d) = i(d) d,
     i(d) = 1 / (d + 10 min)^0.75, blocks placed alternately about the peak position

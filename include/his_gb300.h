@@ -100,6 +100,23 @@ int32_t his_grid_step(his_grid* grid, const his_step_params* params, double* vol
  * (SWE2D._max_rate / max_dt, which reduces over the batch as well). */
 int32_t his_grid_max_rate(his_grid* grid, double* rate, void* stream);
 
+/* Asynchronous forms.  They enqueue the same work on `stream` and return without
+ * waiting for the GPU: host inputs are copied through pinned staging slots owned by
+ * the handle (the caller's arrays may be reused at once), and outputs go to device
+ * memory or page-locked host memory (anything else is HIS_ERR_BAD_ARG), valid once
+ * `stream` has reached the call.  This is how the reference's step keeps its volumes
+ * and mass-balance accumulators on the device (hydrointel/solver/massbalance.py:1-7):
+ * a coupled step then waits on the GPU once, for its CFL rates.
+ *
+ * his_grid_step_async: as his_grid_step; vols (n_members x 5) may be NULL.
+ * Replaces hydrointel/solver/swe2d.py:298-371 (SWE2D.step), whose StepVolumes are
+ * device tensors. */
+int32_t his_grid_step_async(his_grid* grid, const his_step_params* params, double* vols, void* stream);
+
+/* his_grid_max_rate_async: as his_grid_max_rate into `rate` (n_members).
+ * Replaces the reduction of hydrointel/solver/swe2d.py:179-193. */
+int32_t his_grid_max_rate_async(his_grid* grid, double* rate, void* stream);
+
 /* Per-member surface and retained volumes sum(h)*area, sum(s_filled)*area (host out,
  * n_members x 2; synchronises).  Replaces hydrointel/solver/swe2d.py:169-174. */
 int32_t his_grid_volumes(his_grid* grid, double* vols, void* stream);
@@ -155,6 +172,17 @@ int32_t his_net_step(his_net* net, double dt, int32_t n_sub, const double* forci
  * Replaces hydrointel/solver/swe1d.py:253-262 (SWE1D.max_dt). */
 int32_t his_net_max_rate(his_net* net, double* rate, int32_t* any_wet, void* stream);
 
+/* his_net_step_async: as his_net_step (forcing from any host memory, staged); vols
+ * (n_members x 3) may be NULL.  Replaces the substep loop of
+ * hydrointel/solver/coupling.py:216-221, which adds device tensors. */
+int32_t his_net_step_async(his_net* net, double dt, int32_t n_sub, const double* forcing, double* vols,
+                           void* stream);
+
+/* his_net_max_rate_async: per member (rate, wet) into rate_wet (n_members x 2; wet is
+ * 1.0 when any interior cell is wet, else 0.0).  Replaces the reductions of
+ * hydrointel/solver/swe1d.py:253-262. */
+int32_t his_net_max_rate_async(his_net* net, double* rate_wet, void* stream);
+
 /* Per-member channel volume sum(A*dx) over interior cells (host out; synchronises).
  * Replaces hydrointel/solver/swe1d.py:245-247 (SWE1D.volume). */
 int32_t his_net_volume(his_net* net, double* vol, void* stream);
@@ -180,6 +208,11 @@ int32_t his_links_destroy(his_links* links);
  * it receives the per-link volumes (members concatenated, + = 2-D -> 1-D) and the
  * call synchronises.  Replaces hydrointel/solver/coupling.py:73-124 (exchange). */
 int32_t his_exchange(his_links* links, const his_solver_cfg* cfg, double dt, double* V, void* stream);
+
+/* his_exchange_async: as his_exchange; V (total links, device or page-locked host
+ * memory) may be NULL.  The reference's exchange returns V as a device tensor
+ * (hydrointel/solver/coupling.py:73-124). */
+int32_t his_exchange_async(his_links* links, const his_solver_cfg* cfg, double dt, double* V, void* stream);
 
 /* Running per-member totals of exchanged volume since creation or the last reset:
  * n_members x 2 (2-D -> 1-D, 1-D -> 2-D), host out, synchronises.  reset != 0 zeroes

@@ -157,3 +157,35 @@ def test_fp32_production_form_against_fp64():
           f"final volume rel. error {vol_err:.2e}; steps fp64 {r64.steps} fp32 {r32.steps}")
     assert rmse <= 0.01
     assert vol_err < 1e-3
+
+
+@pytest.mark.parametrize("dtype,tol", [(torch.float64, 1e-9), (torch.float32, 1e-5)])
+def test_batched_dropin_equals_members_run_alone(dtype, tol):
+    """The batched drop-in engine (one shared CFL step, the reference's
+    build_engine_batch) against each member built alone and driven through the
+    batch's dt and substep sequence: the same states and mass terms per member."""
+    from his_gb300 import workloads as W
+    from his_gb300.assembly import build_engine, build_engine_batch
+    storms = W.batched_uniform(3)
+    eb = build_engine_batch(storms, dtype=dtype)
+    singles = [build_engine(s, dtype=dtype) for s in storms]
+    t_end = min(s.t_end for s in storms)
+    t = 0.0
+    for k in range(60):
+        dt = min(eb.two.max_dt(), t_end - t)
+        n_sub = max(1, int(np.ceil(dt / eb.one.max_dt() - 1e-9)))
+        t_next = eb.step(t, t_end)
+        assert eb._last_dt == dt, f"step {k}: the step chose another dt"
+        for e in singles:
+            e.step(t, t_end, dt=dt, n_sub=n_sub)
+        t = t_next
+    for b, e in enumerate(singles):
+        for f in ("h", "hu", "hv"):
+            d = H.max_abs(_np(getattr(eb.two, f)[b]), _np(getattr(e.two, f)))
+            assert d <= tol, f"member {b}: {f} differs by {d}"
+        assert H.max_abs(_np(eb.one.A[b]), _np(e.one.A)) <= 10 * tol
+    sb = eb.mb.sources()
+    for b, e in enumerate(singles):
+        s1 = e.mb.sources()
+        for term in s1:
+            assert sb[term][b] == pytest.approx(s1[term], rel=1e-6, abs=1e-3), (b, term)

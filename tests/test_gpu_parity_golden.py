@@ -97,7 +97,7 @@ def test_links_and_exchange_match_reference():
         two.set_state(fx[f"h_in_{i}"], fx[f"hu_in_{i}"], fx[f"hv_in_{i}"])
         one.A = torch.as_tensor(fx[f"A_in_{i}"])
         V = exchange(one, two, links, spec["dt"], SolverConfig())
-        assert H.max_abs(V.numpy(), fx[f"V_{i}"]) <= 1e-12 * max(1.0, float(np.abs(fx[f"V_{i}"]).max()))
+        assert H.max_abs(_np(V), fx[f"V_{i}"]) <= 1e-12 * max(1.0, float(np.abs(fx[f"V_{i}"]).max()))
         for f in ("h", "hu", "hv"):
             assert H.max_abs(_np(getattr(two, f)), fx[f"{f}_out_{i}"]) <= 1e-13, f"call {i}: {f}"
         assert H.max_abs(_np(one.A), fx[f"A_out_{i}"]) <= 1e-12
@@ -129,3 +129,51 @@ def test_coupled_engine_matches_reference():
     for term in ("rain", "infiltration", "bnd2d_in", "bnd2d_out", "bnd1d_in", "bnd1d_out", "clip"):
         assert src[term] == pytest.approx(float(fx[f"src_{term}"]), rel=1e-10, abs=1e-9), term
     assert eng.mb.check(eng.total_volume(), t, record=False) < 1e-12
+
+
+def test_coupled_engine_cfl_choice_matches_reference():
+    """The step choosing its own dt and substep count (both CFL rates fetched with one
+    wait, 1-D substeps on a side stream) reproduces the reference's dt and n_sub
+    sequence and its states."""
+    from his_gb300.coupling import CoupledEngine
+    fx_x = H.load("exchange_overtop")
+    fx = H.load("coupled_overtop")
+    spec = GC.COUPLED_CASES["coupled_overtop"]
+    one, two, links, p = H.cuda_overtop(fx_x)
+    two.set_state(fx["h0"])
+    one.A = torch.as_tensor(fx["A0"])
+    one.Q = torch.as_tensor(fx["Q0"])
+    eng = CoupledEngine(two, one, p.cfg, rain=GC.rain_fn_coupled(spec), links=links)
+    t = 0.0
+    for k in range(spec["steps"]):
+        n_sub_before = eng.log.n_sub_max
+        t = eng.step(t, spec["t_end"])
+        assert eng._last_dt == pytest.approx(float(fx["dt"][k]), rel=1e-12), f"step {k}: dt"
+        assert eng.log.n_sub_max == max(n_sub_before, int(fx["n_sub"][k])), f"step {k}: n_sub"
+        if k + 1 in spec["snap_at"]:
+            for f in ("h", "hu", "hv"):
+                assert H.max_abs(_np(getattr(two, f)), fx[f"{f}_{k + 1}"]) <= 1e-11, f"step {k + 1}: {f}"
+            assert H.max_abs(_np(one.A), fx[f"A_{k + 1}"]) <= 1e-10
+            assert H.max_abs(_np(one.Q), fx[f"Q_{k + 1}"]) <= 1e-10
+    src = eng.mb.sources()
+    for term in ("rain", "infiltration", "bnd2d_in", "bnd2d_out", "bnd1d_in", "bnd1d_out", "clip"):
+        assert src[term] == pytest.approx(float(fx[f"src_{term}"]), rel=1e-10, abs=1e-9), term
+
+
+def test_async_entry_points_refuse_pageable_outputs():
+    """Outputs of the asynchronous entry points must be device or page-locked memory;
+    a pageable array is refused before any work is enqueued."""
+    from his_gb300 import _lib
+    fx_x = H.load("exchange_overtop")
+    one, two, links, p = H.cuda_overtop(fx_x)
+    lib = _lib.load()
+    pageable = np.zeros(max(two.B, 8) * 8)
+    with pytest.raises(ValueError, match="page-locked"):
+        _lib.check(lib.his_grid_max_rate_async(two._handle, pageable.ctypes.data, _lib.stream_handle()), "rate")
+    with pytest.raises(ValueError, match="page-locked"):
+        _lib.check(lib.his_net_max_rate_async(one._handle, pageable.ctypes.data, _lib.stream_handle()), "rate")
+    pinned = torch.zeros(2 * two.B, dtype=torch.float64, pin_memory=True)
+    two.rates_async(pinned[: two.B])
+    one.rates_async(pinned)
+    torch.cuda.synchronize()
+    assert float(pinned[0]) == pytest.approx(float(one.member_rates()[0][0]), rel=0, abs=0)
