@@ -23,8 +23,8 @@ from ._lib import NumericalInstabilityError
 from .boundaries import edge_values
 from .config import SolverConfig
 from .massbalance import MassBalance
-from .swe1d import SWE1D
-from .swe2d import SWE2D
+from .swe1d import SWE1D, Step1DVolumes
+from .swe2d import SWE2D, StepVolumes
 
 log = logging.getLogger("his_gb300.solver")
 
@@ -119,6 +119,7 @@ def exchange(one: SWE1D, two: SWE2D, links: Links, dt: float, cfg: SolverConfig,
     (coupling.py:73-124).  ``volumes=False`` skips them (the coupled step discards them)."""
     V = torch.empty((links.B, links.n_links), dtype=torch.float64, device=two.device) if volumes else None
     cfgc = links.cfg_struct(cfg)
+    one._kernel_writes += 1
     with _lib.on_device(two.device):
         _lib.check(links._lib.his_exchange_async(links._handle, C.byref(cfgc), float(dt),
                                                  V.data_ptr() if V is not None and V.numel() else None,
@@ -173,6 +174,11 @@ class CoupledEngine:
         # the 1-D substeps overlap the 2-D step (disjoint state once the exchange is done)
         self._side = torch.cuda.Stream(two.device) if one is not None else None
         self._exchanged = torch.cuda.Event() if one is not None else None
+        # volumes of the step in flight, added to the mass terms on the device
+        self._vol2d = torch.zeros((two.B, 5), dtype=torch.float64, device=two.device)
+        self._vol1d = torch.zeros((two.B, 3), dtype=torch.float64, device=two.device) if one is not None else None
+        # state version of the 1-D model when its rates were last reduced ahead (None: not)
+        self._rates1_at = None
 
     def check_plausible(self, t: float, label: str = "") -> None:
         h = self.two.h
@@ -206,13 +212,16 @@ class CoupledEngine:
         return v if self.batch is not None else float(v)
 
     def _enqueue_rates(self, need2: bool, need1: bool) -> None:
-        """Both CFL reductions of the current state, into one pinned buffer."""
+        """Both CFL reductions of the current state, into one pinned buffer.  The 1-D
+        rates reduced ahead on the side stream at the end of the last step are the
+        current state's unless A or Q has been written since (state version)."""
         B = self.two.B
         with _lib.on_device(self.two.device):
             if need2:
                 self.two.rates_async(self._rates[:B])
-            if need1:
+            if need1 and self._rates1_at != self.one.state_version():
                 self.one.rates_async(self._rates[B:])
+        self._rates1_at = None
 
     def _wait_rates(self):
         """Largest 2-D rate and (largest 1-D rate, any wet), after one wait for the GPU."""
@@ -239,24 +248,28 @@ class CoupledEngine:
         if wait:
             r2, r1, wet1 = self._wait_rates()
         dt = min(two.dt_from_rate(r2) if dt is None else dt, t_limit - t)
+        main = torch.cuda.current_stream(two.device)
         if one is not None:
             if n_sub is None:
                 n_sub = max(1, math.ceil(dt / one.dt_from_rate(r1, wet1) - 1e-9))
             exchange(one, two, self.links, dt, self.cfg, volumes=False)
-            main = torch.cuda.current_stream(two.device)
             self._exchanged.record(main)
-        vol = two.step(dt, t, rain_t, edges_t=edges_t)
+        two.step_into(dt, t, rain_t, edges_t, self._vol2d.data_ptr(), main.cuda_stream)
         if one is not None:
-            # after the 2-D launch, so the host prepares the substeps while it runs
-            self._side.wait_event(self._exchanged)
-            with torch.cuda.stream(self._side):
-                v1 = one.substeps(dt, t, n_sub)
+            # after the 2-D launch, so the host prepares the substeps while it runs;
+            # the next step's 1-D rates are reduced right behind them, beside the 2-D
+            side = self._side
+            side.wait_event(self._exchanged)
+            one.substeps_into(dt, t, n_sub, self._vol1d.data_ptr(), side.cuda_stream)
+            one.rates_async(self._rates[two.B:], side.cuda_stream)
+            self._rates1_at = one.state_version()
         mb = self.mb
-        mb.add_columns(vol.TERMS, vol.table)
+        mb.add_columns(StepVolumes.TERMS, self._vol2d)
         if one is not None:
             main.wait_stream(self._side)
-            mb.add_columns(v1.TERMS, v1.table)
+            mb.add_columns(Step1DVolumes.TERMS, self._vol1d)
             self.log.n_sub_max = max(self.log.n_sub_max, n_sub)
+            self._last_n_sub = n_sub
         self.log.steps += 1
         self._last_dt = dt
         self.log.dt_min = min(self.log.dt_min, dt)

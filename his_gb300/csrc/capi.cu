@@ -292,7 +292,8 @@ int32_t his_grid_max_rate_async(his_grid* g, double* rate, void* stream) {
     if (rc) return rc;
     cudaStream_t s = (cudaStream_t)stream;
     double* ext = direct ? rate : nullptr;
-    if ((rc = g->prec == HIS_PREC_F64 ? grid_reduce_f64(g, s, ext) : grid_reduce_f32(g, s, ext)) || direct) return rc;
+    rc = g->prec == HIS_PREC_F64 ? grid_reduce_f64(g, s, ext, true) : grid_reduce_f32(g, s, ext, true);
+    if (rc || direct) return rc;
     HIS_CK(cudaMemcpy2DAsync(rate, sizeof(double), g->d_out + 5, 8 * sizeof(double), sizeof(double), g->n,
                              cudaMemcpyDefault, s));
     return HIS_OK;
@@ -301,7 +302,7 @@ int32_t his_grid_max_rate_async(his_grid* g, double* rate, void* stream) {
 int32_t his_grid_max_rate(his_grid* g, double* rate, void* stream) {
     if (!g || !rate) return bad("grid and rate are required");
     cudaStream_t s = (cudaStream_t)stream;
-    int rc = g->prec == HIS_PREC_F64 ? grid_reduce_f64(g, s) : grid_reduce_f32(g, s);
+    int rc = g->prec == HIS_PREC_F64 ? grid_reduce_f64(g, s, nullptr, true) : grid_reduce_f32(g, s, nullptr, true);
     if (rc || (rc = fetch_out(g, s))) return rc;
     for (int m = 0; m < g->n; ++m) rate[m] = g->h_out[m * 8 + 5];
     return HIS_OK;

@@ -126,11 +126,12 @@ int noalloc_step_f32(const Consts& c, const his_grid_desc& d, const his_step_par
 int grid_init_f64(his_grid* g);
 int grid_init_f32(his_grid* g);
 // ext: optional device-writable copy of the outputs (step: 5 volumes per member;
-// reduce: the rate per member), written by the finalize kernel itself
+// reduce: the rate per member), written by the finalize kernel itself; rate_only:
+// the CFL rate alone (d_out's volume columns are left as they were)
 int grid_step_f64(his_grid* g, cudaStream_t s, double* ext = nullptr);
 int grid_step_f32(his_grid* g, cudaStream_t s, double* ext = nullptr);
-int grid_reduce_f64(his_grid* g, cudaStream_t s, double* ext = nullptr);
-int grid_reduce_f32(his_grid* g, cudaStream_t s, double* ext = nullptr);
+int grid_reduce_f64(his_grid* g, cudaStream_t s, double* ext = nullptr, bool rate_only = false);
+int grid_reduce_f32(his_grid* g, cudaStream_t s, double* ext = nullptr, bool rate_only = false);
 int exchange_f64(his_links* l, const Consts& c, double dt, cudaStream_t s);
 int exchange_f32(his_links* l, const Consts& c, double dt, cudaStream_t s);
 size_t stage_smem_bytes(int prec, int tx, int ty);

@@ -5,7 +5,9 @@
 namespace his {
 int grid_init_f32(his_grid* g) { return grid_init_impl<float>(g); }
 int grid_step_f32(his_grid* g, cudaStream_t s, double* ext) { return grid_step_impl<float>(g, s, ext); }
-int grid_reduce_f32(his_grid* g, cudaStream_t s, double* ext) { return grid_reduce_impl<float>(g, s, ext); }
+int grid_reduce_f32(his_grid* g, cudaStream_t s, double* ext, bool rate_only) {
+    return grid_reduce_impl<float>(g, s, ext, rate_only);
+}
 int exchange_f32(his_links* l, const Consts& c, double dt, cudaStream_t s) { return exchange_impl<float>(l, c, dt, s); }
 size_t stage_smem_bytes(int prec, int tx, int ty) {
     (void)ty;

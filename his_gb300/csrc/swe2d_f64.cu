@@ -5,7 +5,9 @@
 namespace his {
 int grid_init_f64(his_grid* g) { return grid_init_impl<double>(g); }
 int grid_step_f64(his_grid* g, cudaStream_t s, double* ext) { return grid_step_impl<double>(g, s, ext); }
-int grid_reduce_f64(his_grid* g, cudaStream_t s, double* ext) { return grid_reduce_impl<double>(g, s, ext); }
+int grid_reduce_f64(his_grid* g, cudaStream_t s, double* ext, bool rate_only) {
+    return grid_reduce_impl<double>(g, s, ext, rate_only);
+}
 int exchange_f64(his_links* l, const Consts& c, double dt, cudaStream_t s) { return exchange_impl<double>(l, c, dt, s); }
 int engine_enqueue_f64(his_engine* e, int n) { return engine_enqueue_impl<double>(e, n); }
 int engine_take_rate_f64(his_engine* e) { return engine_take_rate_impl<double>(e); }

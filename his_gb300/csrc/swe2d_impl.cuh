@@ -50,11 +50,15 @@ int launch_step_nt(his_grid* g, cudaStream_t s, double* ext) {
 }
 
 template <class R, int NT>
-int launch_reduce_nt(his_grid* g, cudaStream_t s, double* ext) {
+int launch_reduce_nt(his_grid* g, cudaStream_t s, double* ext, bool rate_only) {
     auto* grids = reinterpret_cast<const Grid<R>*>(g->d_grids);
-    strip_reduce_kernel<R, NT><<<g->n_tiles, NT, 0, s>>>(grids, reinterpret_cast<const StripRef*>(g->d_tiles),
-                                                         make_kc<R>(g->c), g->d_partials);
-    finalize_kernel<R><<<g->n, 32, 0, s>>>(grids, g->d_params, g->c, g->d_partials, g->d_out, 1, ext);
+    auto* strips = reinterpret_cast<const StripRef*>(g->d_tiles);
+    if (rate_only)
+        strip_rate_kernel<R, NT><<<g->n_tiles, NT, 0, s>>>(grids, strips, make_kc<R>(g->c), g->d_partials);
+    else
+        strip_reduce_kernel<R, NT><<<g->n_tiles, NT, 0, s>>>(grids, strips, make_kc<R>(g->c), g->d_partials);
+    finalize_kernel<R><<<g->n, 32, 0, s>>>(grids, g->d_params, g->c, g->d_partials, g->d_out, rate_only ? 2 : 1,
+                                           ext);
     HIS_CK(cudaGetLastError());
     return HIS_OK;
 }
@@ -149,8 +153,8 @@ int grid_step_impl(his_grid* g, cudaStream_t s, double* ext) {
 }
 
 template <class R>
-int grid_reduce_impl(his_grid* g, cudaStream_t s, double* ext) {
-    HIS_NT_DISPATCH(launch_reduce_nt, R, g, s, ext);
+int grid_reduce_impl(his_grid* g, cudaStream_t s, double* ext, bool rate_only) {
+    HIS_NT_DISPATCH(launch_reduce_nt, R, g, s, ext, rate_only);
 }
 
 template <class R>
@@ -213,7 +217,7 @@ int engine_take_rate_impl(his_engine* E) {
     // kernel attributes are set here, outside any stream capture
     if (E->pre_smem > 48 * 1024)
         HIS_CK(cudaFuncSetAttribute(eng_pre_kernel<R>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)E->pre_smem));
-    int rc = grid_reduce_impl<R>(E->grid, E->s0, nullptr);
+    int rc = grid_reduce_impl<R>(E->grid, E->s0, nullptr, false);
     if (rc) return rc;
     eng_take_rate_kernel<<<(E->n + 127) / 128, 128, 0, E->s0>>>(E->d_em, E->grid->d_out, E->n);
     HIS_CK(cudaGetLastError());

@@ -587,9 +587,43 @@ __global__ void __launch_bounds__(NT) strip_reduce_kernel(const Grid<R>* __restr
     block_reduce_store<3>(v, mx, red, partials + (size_t)blockIdx.x * NPART, sl, NT);
 }
 
+// Per strip-chunk CFL rate alone (swe2d.py:179-184), for the step's dt: the maximum
+// is exact in the compute type, so the cells need no float64 work (slow on this GPU)
+// and the result equals strip_reduce_kernel's; rows are unrolled to keep loads in
+// flight.  Writes only the P_RATE partial.
+template <class R, int NT>
+__global__ void __launch_bounds__(NT) strip_rate_kernel(const Grid<R>* __restrict__ grids,
+                                                         const StripRef* __restrict__ strips, const KC<R> c,
+                                                         double* __restrict__ partials) {
+    __shared__ R red[32];
+    const StripRef sr = strips[blockIdx.x];
+    const Grid<R>& gd = grids[sr.member];
+    R rate = R(0);
+    const int cx = sr.x0 + threadIdx.x;
+    if ((int)threadIdx.x < sr.w && cx < gd.nx) {
+        const int y1 = min(sr.y1, gd.ny);
+#pragma unroll 4
+        for (int y = sr.y0; y < y1; ++y) {
+            const size_t i = (size_t)y * gd.nx + cx;
+            R h = gd.h[i], u, v;
+            kp_velocity(c, h, gd.hu[i], gd.hv[i], u, v);
+            const R cw = dsqrt(c.g * h);
+            const R r = h > c.h_dry ? per_len(fabs(u) + cw, gd.rdx, gd.idx) + per_len(fabs(v) + cw, gd.rdy, gd.idy)
+                                    : R(0);
+            rate = rmax(rate, r);
+        }
+    }
+    R v[1] = {rate};
+    const bool mx[1] = {true};
+    const int sl[1] = {P_RATE};
+    block_reduce_store<1>(v, mx, red, partials + (size_t)blockIdx.x * NPART, sl, NT);
+}
+
 // Per-member totals from the strip-chunk partials, in a fixed order.  out: 8 per
 // member = bnd_in, bnd_out, rain, infil, clip (m^3), rate (1/s), surface and retained
-// volume.  mode 0: after a step; mode 1: rate and volumes only.
+// volume.  mode 0: after a step; mode 1: rate and volumes only; mode 2: rate only
+// (after strip_rate_kernel).  ext (optional, device-writable): mode 0 the 5 volumes,
+// modes 1 and 2 the rate, per member.
 template <class R>
 __global__ void finalize_kernel(const Grid<R>* __restrict__ grids, const StepParams* __restrict__ params, Consts c,
                                 const double* __restrict__ partials, double* __restrict__ out, int mode,
@@ -597,6 +631,16 @@ __global__ void finalize_kernel(const Grid<R>* __restrict__ grids, const StepPar
     const int m = blockIdx.x, lane = threadIdx.x;
     const Grid<R>& gd = grids[m];
     if (mode == 0 && !params[m].active) return;
+    if (mode == 2) {
+        double r = 0.0;
+        for (int t = lane; t < gd.n_tiles; t += 32) r = fmax(r, partials[(size_t)(gd.tile0 + t) * NPART + P_RATE]);
+        r = warp_max(r);
+        if (lane == 0) {
+            out[(size_t)m * 8 + 5] = r;
+            if (ext) ext[m] = r;
+        }
+        return;
+    }
     double s[NPART];
 #pragma unroll
     for (int j = 0; j < NPART; ++j) s[j] = 0.0;

@@ -107,6 +107,7 @@ class SWE1D:
         self.interior = ~self.is_ghost
         self.a_dry = self.sec.area(torch.full_like(self.z, cfg.h_dry))
         self.inflow, self.stage = inflow, stage
+        self._kernel_writes = 0
         self._A = torch.zeros(self.bshape + (tp.n_cells,), dtype=torch.float64, device=self.device)
         self._Q = torch.zeros_like(self._A)
         self._lib = _lib.load()
@@ -179,11 +180,12 @@ class SWE1D:
                                                   _lib.stream_handle()), "his_net_max_rate")
         return rate, wet
 
-    def rates_async(self, out: torch.Tensor) -> None:
+    def rates_async(self, out: torch.Tensor, stream: int | None = None) -> None:
         """Enqueue per-member (rate, wet) into ``out`` (B x 2 float64, device or pinned
-        host memory), valid once the current stream reaches this point."""
+        host memory), valid once ``stream`` (default: the current one) reaches this point."""
         with _lib.on_device(self.device):
-            _lib.check(self._lib.his_net_max_rate_async(self._handle, out.data_ptr(), _lib.stream_handle()),
+            _lib.check(self._lib.his_net_max_rate_async(self._handle, out.data_ptr(),
+                                                        _lib.stream_handle() if stream is None else stream),
                        "his_net_max_rate_async")
 
     def max_dt(self) -> float:
@@ -205,15 +207,27 @@ class SWE1D:
     def substeps(self, dt: float, t: float, n_sub: int) -> Step1DVolumes:
         """n_sub substeps of dt/n_sub, forcing evaluated at each substep start
         (coupling.py:216-221), in one launch."""
-        sub = dt / n_sub
-        f = np.stack([self.forcing(t + k * sub) for k in range(n_sub)], axis=1)   # (B, n_sub, 2)
-        f = np.ascontiguousarray(f, dtype=np.float64)
         vols = torch.empty((self.B, 3), dtype=torch.float64, device=self.device)
-        with _lib.on_device(self.device):
-            _lib.check(self._lib.his_net_step_async(self._handle, float(dt), int(n_sub), _lib.as_p(f),
-                                                    vols.data_ptr(), _lib.stream_handle()), "his_net_step_async")
+        self.substeps_into(dt, t, n_sub, vols.data_ptr())
         cols = vols.t().unbind(0) if self.bshape else vols[0].unbind(0)
         return Step1DVolumes(*cols, table=vols)
+
+    def substeps_into(self, dt: float, t: float, n_sub: int, vols_ptr: int, stream: int | None = None) -> None:
+        """The substeps with their (B, 3) float64 volumes written to ``vols_ptr`` (device
+        or page-locked memory) on ``stream`` (default: the current stream)."""
+        sub = dt / n_sub
+        f = self.forcing(t) if n_sub == 1 else np.stack([self.forcing(t + k * sub) for k in range(n_sub)], axis=1)
+        f = np.ascontiguousarray(f, dtype=np.float64)
+        self._kernel_writes += 1
+        with _lib.on_device(self.device):
+            _lib.check(self._lib.his_net_step_async(self._handle, float(dt), int(n_sub), _lib.as_p(f), vols_ptr,
+                                                    _lib.stream_handle() if stream is None else stream),
+                       "his_net_step_async")
+
+    def state_version(self) -> tuple:
+        """Changes whenever A or Q is written: through torch (assignment, in-place ops)
+        or by this library's substeps and exchange."""
+        return (self._A._version, self._Q._version, self._kernel_writes)
 
     def step(self, dt: float, t: float) -> Step1DVolumes:
         return self.substeps(dt, t, 1)

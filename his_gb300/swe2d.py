@@ -53,8 +53,11 @@ _STEP_DTYPE = np.dtype(_lib.StepParams)
 
 def per_member(values, B: int, dtype=np.float64) -> np.ndarray:
     """1 value (broadcast) or one per member, else ValueError (swe2d.py:282-296)."""
-    if all(isinstance(v, (float, int)) for v in values):
-        return np.repeat(np.asarray(values, dtype=dtype)[:, None], B, axis=1)
+    if all(isinstance(v, (float, int)) or (isinstance(v, np.ndarray) and v.size in (1, B)) for v in values):
+        out = np.empty((len(values), B), dtype=dtype)
+        for k, v in enumerate(values):
+            out[k] = v.reshape(-1) if isinstance(v, np.ndarray) else v
+        return out
     out = []
     for v in values:
         if torch.is_tensor(v):
@@ -132,6 +135,8 @@ class SWE2D:
             d.f0, d.fc, d.k = self._plane(self._f0, b), self._plane(self._fc, b), self._plane(self._k, b)
             d.rain_weight = self._plane(self.rain_weight, b)
         tx, ty = tile if tile is not None else (0, 0)
+        self._params_rec = np.zeros(self.B, dtype=_STEP_DTYPE)
+        self._params_ptr = self._params_rec.ctypes.data_as(C.POINTER(_lib.StepParams))
         cfgc = _lib.solver_cfg(cfg)
         with _lib.on_device(self.device):
             _lib.check(self._lib.his_grid_create(self.prec, C.byref(cfgc), self.B, descs, int(tx), int(ty),
@@ -228,25 +233,33 @@ class SWE2D:
     def step_params(self, dt: float, t: float, rain_rate=0.0, edges_t=None):
         """his_step_params of every member, as a numpy record array with the C layout
         (filled column-wise: a Python loop over members costs more than a GPU step).
-        ``edges_t``: the edge values at t, when the caller has them already."""
+        ``edges_t``: the edge values at t, when the caller has them already.
+        The records live in one buffer per solver, refilled by every call: the pointer
+        returned is valid until the next call (the C entry points copy the records
+        before returning)."""
         at_t = edge_values(self.bcs, t) if edges_t is None else edges_t
         pm = per_member([rain_rate] + at_t + edge_values(self.bcs, t + dt), self.B)
-        a = np.empty(self.B, dtype=_STEP_DTYPE)
+        a = self._params_rec
         a["dt"], a["t"], a["rain"] = float(dt), float(t), pm[0]
         a["bc_t"], a["bc_t_dt"] = pm[1:5].T, pm[5:9].T
-        self._params_keep = a
-        return a.ctypes.data_as(C.POINTER(_lib.StepParams))
+        return self._params_ptr
 
     def step(self, dt: float, t: float, rain_rate=0.0, edges_t=None) -> StepVolumes:
         """One SSP-RK2 step, enqueued on the current stream without waiting for it; the
         volumes are float64 device tensors, as the reference's are."""
-        params = self.step_params(dt, t, rain_rate, edges_t)
         vols = torch.empty((self.B, 5), dtype=torch.float64, device=self.device)
-        with _lib.on_device(self.device):
-            _lib.check(self._lib.his_grid_step_async(self._handle, params, vols.data_ptr(), _lib.stream_handle()),
-                       "his_grid_step_async")
+        self.step_into(dt, t, rain_rate, edges_t, vols.data_ptr())
         cols = vols.t().unbind(0) if self.bshape else vols[0].unbind(0)
         return StepVolumes(*cols, table=vols)
+
+    def step_into(self, dt: float, t: float, rain_rate, edges_t, vols_ptr: int, stream: int | None = None) -> None:
+        """The step with its (B, 5) float64 volumes written to ``vols_ptr`` (device or
+        page-locked memory) on ``stream`` (default: the current stream)."""
+        params = self.step_params(dt, t, rain_rate, edges_t)
+        with _lib.on_device(self.device):
+            _lib.check(self._lib.his_grid_step_async(self._handle, params, vols_ptr,
+                                                     _lib.stream_handle() if stream is None else stream),
+                       "his_grid_step_async")
 
     def scratch_bytes(self) -> int:
         return int(self._lib.his_grid_scratch_bytes(self._handle))

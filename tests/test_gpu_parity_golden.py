@@ -177,3 +177,35 @@ def test_async_entry_points_refuse_pageable_outputs():
     one.rates_async(pinned)
     torch.cuda.synchronize()
     assert float(pinned[0]) == pytest.approx(float(one.member_rates()[0][0]), rel=0, abs=0)
+
+
+def test_coupled_step_sees_state_written_between_steps():
+    """The 1-D rates reduced ahead at the end of a step are dropped when the 1-D state
+    is written before the next one (through torch, or by a standalone exchange): the
+    next step's substep count is that of the written state."""
+    import math
+    from his_gb300.coupling import CoupledEngine, exchange
+    fx_x = H.load("exchange_overtop")
+    fx = H.load("coupled_overtop")
+    spec = GC.COUPLED_CASES["coupled_overtop"]
+    one, two, links, p = H.cuda_overtop(fx_x)
+    two.set_state(fx["h0"])
+    one.A = torch.as_tensor(fx["A0"])
+    one.Q = torch.as_tensor(fx["Q0"])
+    eng = CoupledEngine(two, one, p.cfg, rain=GC.rain_fn_coupled(spec), links=links)
+    t = 0.0
+    for _ in range(3):
+        t = eng.step(t, spec["t_end"])
+
+    def expected(t):
+        dt = min(two.dt_from_rate(float(two.member_rates().max())), spec["t_end"] - t)
+        return dt, max(1, math.ceil(dt / one.max_dt() - 1e-9))
+
+    one.A = one.A * 4.0                          # deeper channel: faster 1-D waves
+    dt, n_sub = expected(t)
+    t = eng.step(t, spec["t_end"])
+    assert eng._last_dt == dt and eng._last_n_sub == n_sub
+    exchange(one, two, links, 30.0, p.cfg)       # the library writes A itself
+    dt, n_sub = expected(t)
+    t = eng.step(t, spec["t_end"])
+    assert eng._last_dt == dt and eng._last_n_sub == n_sub
