@@ -649,16 +649,21 @@ int32_t his_engine_destroy(his_engine* E) {
     if (!E) return HIS_OK;
     if (E->s0) cudaStreamSynchronize(E->s0);
     if (E->s1) cudaStreamSynchronize(E->s1);
+    for (cudaStream_t s : E->cs)
+        if (s) cudaStreamSynchronize(s);
     if (E->exec) cudaGraphExecDestroy(E->exec);
+    if (E->cexec) cudaGraphExecDestroy(E->cexec);
     cudaFree(E->d_em);
     cudaFree(E->d_arena);
     cudaFree(E->d_netf);
     cudaFree(E->d_vol1d);
     if (E->h_em) cudaFreeHost(E->h_em);
-    for (cudaEvent_t ev : {E->ev_fork, E->ev_join, E->ev_in, E->ev_out})
+    for (cudaEvent_t ev : {E->ev_fork, E->ev_join, E->ev_in, E->ev_out, E->cev_fork, E->cev_join, E->cev_out})
         if (ev) cudaEventDestroy(ev);
     if (E->s0) cudaStreamDestroy(E->s0);
     if (E->s1) cudaStreamDestroy(E->s1);
+    for (cudaStream_t s : E->cs)
+        if (s) cudaStreamDestroy(s);
     delete E;
     return HIS_OK;
 }
@@ -742,6 +747,21 @@ int32_t his_engine_create(his_grid* grid, his_net* net, his_links* links, int32_
     if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&E->s1, cudaStreamNonBlocking);
     for (cudaEvent_t* ev : {&E->ev_fork, &E->ev_join, &E->ev_in, &E->ev_out})
         if (e == cudaSuccess) e = cudaEventCreateWithFlags(ev, cudaEventDisableTiming);
+    // two chains split where the tiles are halved (at least one member each)
+    E->n_chains = n_members >= 2 ? 2 : 1;
+    if (E->n_chains == 2) {
+        int mid = 1;
+        while (mid < n_members - 1 && grid->tile0[mid] < grid->n_tiles / 2) ++mid;
+        E->chain_m[0] = 0; E->chain_m[1] = mid; E->chain_m[2] = n_members;
+        E->chain_t[0] = 0; E->chain_t[1] = grid->tile0[mid]; E->chain_t[2] = grid->n_tiles;
+        for (cudaStream_t& s : E->cs)
+            if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking);
+        for (cudaEvent_t* ev : {&E->cev_fork, &E->cev_join, &E->cev_out})
+            if (e == cudaSuccess) e = cudaEventCreateWithFlags(ev, cudaEventDisableTiming);
+    } else {
+        E->chain_m[0] = 0; E->chain_m[1] = E->chain_m[2] = n_members;
+        E->chain_t[0] = 0; E->chain_t[1] = E->chain_t[2] = grid->n_tiles;
+    }
     if (e != cudaSuccess) return fail(e, "his_engine_create: allocation");
     int rc = net_engine_prepare(E);
     if (rc == HIS_OK) rc = grid->prec == HIS_PREC_F64 ? engine_take_rate_f64(E) : engine_take_rate_f32(E);
@@ -757,37 +777,58 @@ int32_t his_engine_create(his_grid* grid, his_net* net, his_links* links, int32_
     return HIS_OK;
 }
 
-static int engine_enqueue(his_engine* E, int n) {
-    return E->grid->prec == HIS_PREC_F64 ? engine_enqueue_f64(E, n) : engine_enqueue_f32(E, n);
+static int engine_enqueue(his_engine* E, int chain, int n) {
+    return E->grid->prec == HIS_PREC_F64 ? engine_enqueue_f64(E, chain, n) : engine_enqueue_f32(E, chain, n);
+}
+
+// One graph of graph_steps steps of one chain, captured from the chain's main stream.
+static int engine_capture(his_engine* E, int chain, cudaGraphExec_t* exec) {
+    cudaStream_t s = chain == 0 ? E->s0 : E->cs[0];
+    cudaGraph_t graph = nullptr;
+    HIS_CK(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
+    int rc = engine_enqueue(E, chain, E->graph_steps);
+    cudaError_t ce = cudaStreamEndCapture(s, &graph);
+    if (rc) { if (graph) cudaGraphDestroy(graph); return rc; }
+    if (ce != cudaSuccess) return cuda_fail(ce, "his_engine_advance: capture");
+    ce = cudaGraphInstantiate(exec, graph, 0);
+    cudaGraphDestroy(graph);
+    if (ce != cudaSuccess) { *exec = nullptr; return cuda_fail(ce, "his_engine_advance: instantiate"); }
+    return HIS_OK;
 }
 
 int32_t his_engine_advance(his_engine* E, int32_t n_steps, void* stream) {
     if (!E) return bad("engine is NULL");
     if (n_steps < 0) return bad("n_steps must be >= 0");
     cudaStream_t caller = (cudaStream_t)stream;
+    const bool two = E->n_chains == 2;
     HIS_CK(cudaEventRecord(E->ev_in, caller));
     HIS_CK(cudaStreamWaitEvent(E->s0, E->ev_in, 0));
+    if (two) HIS_CK(cudaStreamWaitEvent(E->cs[0], E->ev_in, 0));
     if (!E->exec && n_steps >= E->graph_steps) {
-        cudaGraph_t graph = nullptr;
-        HIS_CK(cudaStreamBeginCapture(E->s0, cudaStreamCaptureModeThreadLocal));
-        int rc = engine_enqueue(E, E->graph_steps);
-        cudaError_t ce = cudaStreamEndCapture(E->s0, &graph);
-        if (rc) { if (graph) cudaGraphDestroy(graph); return rc; }
-        if (ce != cudaSuccess) return cuda_fail(ce, "his_engine_advance: capture");
-        ce = cudaGraphInstantiate(&E->exec, graph, 0);
-        cudaGraphDestroy(graph);
-        if (ce != cudaSuccess) { E->exec = nullptr; return cuda_fail(ce, "his_engine_advance: instantiate"); }
+        int rc = engine_capture(E, 0, &E->exec);
+        if (rc == HIS_OK && two) rc = engine_capture(E, 1, &E->cexec);
+        if (rc) return rc;
     }
+    // the chains run independently until the end of the call, each launching its
+    // graphs back to back on its own stream, so their relative phase is kept
     int done = 0;
     if (E->exec) {
-        for (; done + E->graph_steps <= n_steps; done += E->graph_steps) HIS_CK(cudaGraphLaunch(E->exec, E->s0));
+        for (; done + E->graph_steps <= n_steps; done += E->graph_steps) {
+            HIS_CK(cudaGraphLaunch(E->exec, E->s0));
+            if (two) HIS_CK(cudaGraphLaunch(E->cexec, E->cs[0]));
+        }
     }
     if (done < n_steps) {
-        int rc = engine_enqueue(E, n_steps - done);
+        int rc = engine_enqueue(E, 0, n_steps - done);
+        if (rc == HIS_OK && two) rc = engine_enqueue(E, 1, n_steps - done);
         if (rc) return rc;
     }
     HIS_CK(cudaEventRecord(E->ev_out, E->s0));
     HIS_CK(cudaStreamWaitEvent(caller, E->ev_out, 0));
+    if (two) {
+        HIS_CK(cudaEventRecord(E->cev_out, E->cs[0]));
+        HIS_CK(cudaStreamWaitEvent(caller, E->cev_out, 0));
+    }
     return HIS_OK;
 }
 

@@ -1,6 +1,7 @@
 // Device-resident coupled time loop: every member advances with its own dt, chosen,
 // forced and accounted for on the GPU, so K steps run as one CUDA graph with no
-// host round trip.  One step is
+// host round trip.  The per-member kernels take the first member m0 of the chain
+// they serve (block b works on member m0 + b).  One step is
 //
 //   eng_pre   (one CTA per member)  2-D CFL dt from the rate of the current state,
 //             1-D CFL and substep count, weir exchange, forcing at t, t+dt and at the
@@ -27,11 +28,11 @@ template <class R>
 __global__ void eng_pre_kernel(EngMember* __restrict__ em, StepParams* __restrict__ params,
                                const Grid<R>* __restrict__ grids, const Net* __restrict__ nets,
                                const Lnk* __restrict__ links, Consts c, double* __restrict__ netf, int max_sub,
-                               double* __restrict__ exch) {
+                               double* __restrict__ exch, int m0) {
     extern __shared__ double sm[];
     __shared__ int s_go, s_nsub, s_snap;
     __shared__ double s_dt;
-    const int m = blockIdx.x;
+    const int m = m0 + blockIdx.x;
     EngMember& E = em[m];
     if (threadIdx.x == 0) {
         s_go = E.status == ST_RUNNING;
@@ -107,8 +108,8 @@ __global__ void eng_pre_kernel(EngMember* __restrict__ em, StepParams* __restric
 template <class R>
 __global__ void eng_post_kernel(EngMember* __restrict__ em, const StepParams* __restrict__ params,
                                 const Grid<R>* __restrict__ grids, Consts c, const double* __restrict__ partials,
-                                const double* __restrict__ vol1d, double* __restrict__ out) {
-    const int m = blockIdx.x, lane = threadIdx.x;
+                                const double* __restrict__ vol1d, double* __restrict__ out, int m0) {
+    const int m = m0 + blockIdx.x, lane = threadIdx.x;
     if (!params[m].active) return;
     const Grid<R>& gd = grids[m];
     double s[NPART];

@@ -81,6 +81,15 @@ struct his_engine {
     cudaStream_t s0 = nullptr, s1 = nullptr;
     cudaEvent_t ev_fork = nullptr, ev_join = nullptr, ev_in = nullptr, ev_out = nullptr;
     cudaGraphExec_t exec = nullptr;
+    // The members run as n_chains independent chains (members [chain_m[c], chain_m[c+1]),
+    // tiles [chain_t[c], chain_t[c+1])), each with its own streams and graph, so one
+    // chain's latency-bound pre/post kernels overlap the other's 2-D stages.  Chain 0
+    // uses s0/s1 and the events above; chain 1 uses cs[0]/cs[1] and cev[].
+    int n_chains = 1;
+    int chain_m[3] = {0, 0, 0}, chain_t[3] = {0, 0, 0};
+    cudaStream_t cs[2] = {nullptr, nullptr};
+    cudaEvent_t cev_fork = nullptr, cev_join = nullptr, cev_out = nullptr;
+    cudaGraphExec_t cexec = nullptr;
 };
 
 namespace his {
@@ -136,8 +145,9 @@ int exchange_f64(his_links* l, const Consts& c, double dt, cudaStream_t s);
 int exchange_f32(his_links* l, const Consts& c, double dt, cudaStream_t s);
 size_t stage_smem_bytes(int prec, int tx, int ty);
 
-int engine_enqueue_f64(his_engine* e, int n_steps);
-int engine_enqueue_f32(his_engine* e, int n_steps);
+// n_steps engine steps of chain `chain` on its own streams
+int engine_enqueue_f64(his_engine* e, int chain, int n_steps);
+int engine_enqueue_f32(his_engine* e, int chain, int n_steps);
 int engine_take_rate_f64(his_engine* e);
 int engine_take_rate_f32(his_engine* e);
 int engine_profile_f64(his_engine* e, int n_steps, double* ms);
@@ -147,7 +157,7 @@ int engine_profile_f32(his_engine* e, int n_steps, double* ms);
 // vols / rate_wet: optional device-writable outputs (3 per member; rate and wet per member)
 int net_step_launch(his_net* n, double dt, int n_sub, cudaStream_t s, double* vols = nullptr);
 int net_reduce_launch(his_net* n, cudaStream_t s, double* rate_wet = nullptr);
-int net_engine_launch(his_engine* e, cudaStream_t s);
+int net_engine_launch(his_engine* e, cudaStream_t s, int m0, int count);
 int net_engine_prepare(his_engine* e);
 
 }  // namespace his

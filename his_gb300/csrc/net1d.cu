@@ -55,9 +55,9 @@ __global__ void net_reduce_kernel(const Net* __restrict__ nets, Consts c, double
 // device (written by the engine's pre kernel); members not stepping are skipped.
 __global__ void net_engine_kernel(const Net* __restrict__ nets, Consts c, const EngMember* __restrict__ em,
                                   const StepParams* __restrict__ params, const double* __restrict__ netf, int max_sub,
-                                  double* __restrict__ vol1d) {
+                                  double* __restrict__ vol1d, int m0) {
     extern __shared__ double sm[];
-    const int m = blockIdx.x;
+    const int m = m0 + blockIdx.x;
     if (!params[m].active) return;
     const EngMember& E = em[m];
     const StepParams& P = params[m];
@@ -72,10 +72,10 @@ int net_engine_prepare(his_engine* e) {
     return HIS_OK;
 }
 
-int net_engine_launch(his_engine* e, cudaStream_t s) {
+int net_engine_launch(his_engine* e, cudaStream_t s, int m0, int count) {
     his_net* n = e->net;
-    net_engine_kernel<<<e->n, 128, n->smem, s>>>(n->d_nets, n->c, e->d_em, e->grid->d_params, e->d_netf, e->max_sub,
-                                                 e->d_vol1d);
+    net_engine_kernel<<<count, 128, n->smem, s>>>(n->d_nets, n->c, e->d_em, e->grid->d_params, e->d_netf, e->max_sub,
+                                                  e->d_vol1d, m0);
     HIS_CK(cudaGetLastError());
     return HIS_OK;
 }

@@ -14,7 +14,7 @@ size_t stage_smem_bytes(int prec, int tx, int ty) {
     const int nt = strip_threads(tx);
     return prec == HIS_PREC_F64 ? stage_smem_impl<double>(nt) : stage_smem_impl<float>(nt);
 }
-int engine_enqueue_f32(his_engine* e, int n) { return engine_enqueue_impl<float>(e, n); }
+int engine_enqueue_f32(his_engine* e, int chain, int n) { return engine_enqueue_impl<float>(e, chain, n); }
 int engine_take_rate_f32(his_engine* e) { return engine_take_rate_impl<float>(e); }
 int engine_profile_f32(his_engine* e, int n, double* ms) { return engine_profile_impl<float>(e, n, ms); }
 int noalloc_step_f32(const Consts& c, const his_grid_desc& d, const his_step_params& p, const NoallocPlan& L,

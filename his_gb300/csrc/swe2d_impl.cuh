@@ -21,19 +21,23 @@ int set_strip_attrs() {
     return HIS_OK;
 }
 
-// The 2-D stages of one step on stream s (no finalize).
+// The 2-D stages of one step on stream s (no finalize), over tiles [t0, t0 + count)
+// (default: all); a tile's partials sit at its global index.
 template <class R, int NT>
-int launch_stages(his_grid* g, cudaStream_t s) {
+int launch_stages(his_grid* g, cudaStream_t s, int t0 = 0, int count = -1) {
     using G = StripGeom<R, NT>;
+    if (count < 0) count = g->n_tiles - t0;
+    if (count == 0) return HIS_OK;
     auto* grids = reinterpret_cast<const Grid<R>*>(g->d_grids);
     const KC<R> kc = make_kc<R>(g->c);
-    auto* strips = reinterpret_cast<const StripRef*>(g->d_tiles);
+    auto* strips = reinterpret_cast<const StripRef*>(g->d_tiles) + t0;
+    double* part = g->d_partials + (size_t)t0 * NPART;
     if (g->c.order == 2) {
-        strip_kernel<R, NT, 1><<<g->n_tiles, NT, G::smem_bytes, s>>>(grids, strips, g->d_params, kc, g->d_partials);
-        strip_kernel<R, NT, 2><<<g->n_tiles, NT, G::smem_bytes, s>>>(grids, strips, g->d_params, kc, g->d_partials);
+        strip_kernel<R, NT, 1><<<count, NT, G::smem_bytes, s>>>(grids, strips, g->d_params, kc, part);
+        strip_kernel<R, NT, 2><<<count, NT, G::smem_bytes, s>>>(grids, strips, g->d_params, kc, part);
     } else {
-        strip_kernel<R, NT, 0><<<g->n_tiles, NT, G::smem_bytes, s>>>(grids, strips, g->d_params, kc, g->d_partials);
-        stage_copy_kernel<R, NT><<<g->n_tiles, NT, 0, s>>>(grids, strips, g->d_params);
+        strip_kernel<R, NT, 0><<<count, NT, G::smem_bytes, s>>>(grids, strips, g->d_params, kc, part);
+        stage_copy_kernel<R, NT><<<count, NT, 0, s>>>(grids, strips, g->d_params);
     }
     HIS_CK(cudaGetLastError());
     return HIS_OK;
@@ -177,39 +181,44 @@ size_t stage_smem_impl(int nt) {
     return 0;
 }
 
-// One device-resident step for every member (see engine_kernels.cuh); the 1-D
-// substeps run on the side stream between a fork and a join event, concurrently
-// with the 2-D stages.
+// One device-resident step for every member of one chain (see engine_kernels.cuh)
+// on the chain's main stream; the 1-D substeps run on its side stream between a
+// fork and a join event, concurrently with the 2-D stages.
 template <class R, int NT>
-int eng_enqueue_nt(his_grid* g, his_engine* E, int n_steps) {
+int eng_enqueue_nt(his_grid* g, his_engine* E, int chain, int n_steps) {
     auto* grids = reinterpret_cast<const Grid<R>*>(g->d_grids);
     const Net* nets = E->net ? E->net->d_nets : nullptr;
     const Lnk* links = E->links ? E->links->d_links : nullptr;
     double* exch = E->links ? E->links->d_exch : nullptr;
+    const int m0 = E->chain_m[chain], mc = E->chain_m[chain + 1] - m0;
+    const int t0 = E->chain_t[chain], tc = E->chain_t[chain + 1] - t0;
+    cudaStream_t s_main = chain == 0 ? E->s0 : E->cs[0], s_side = chain == 0 ? E->s1 : E->cs[1];
+    cudaEvent_t fork = chain == 0 ? E->ev_fork : E->cev_fork, join = chain == 0 ? E->ev_join : E->cev_join;
+    if (mc == 0) return HIS_OK;
     for (int k = 0; k < n_steps; ++k) {
-        eng_pre_kernel<R><<<E->n, ENG_PRE_THREADS, E->pre_smem, E->s0>>>(E->d_em, g->d_params, grids, nets, links, g->c,
-                                                             E->d_netf, E->max_sub, exch);
+        eng_pre_kernel<R><<<mc, ENG_PRE_THREADS, E->pre_smem, s_main>>>(E->d_em, g->d_params, grids, nets, links, g->c,
+                                                                        E->d_netf, E->max_sub, exch, m0);
         if (E->net) {
-            HIS_CK(cudaEventRecord(E->ev_fork, E->s0));
-            HIS_CK(cudaStreamWaitEvent(E->s1, E->ev_fork, 0));
-            int rc = net_engine_launch(E, E->s1);
+            HIS_CK(cudaEventRecord(fork, s_main));
+            HIS_CK(cudaStreamWaitEvent(s_side, fork, 0));
+            int rc = net_engine_launch(E, s_side, m0, mc);
             if (rc) return rc;
-            HIS_CK(cudaEventRecord(E->ev_join, E->s1));
+            HIS_CK(cudaEventRecord(join, s_side));
         }
-        int rc = launch_stages<R, NT>(g, E->s0);
+        int rc = launch_stages<R, NT>(g, s_main, t0, tc);
         if (rc) return rc;
-        if (E->net) HIS_CK(cudaStreamWaitEvent(E->s0, E->ev_join, 0));
-        eng_post_kernel<R><<<E->n, 32, 0, E->s0>>>(E->d_em, g->d_params, grids, g->c, g->d_partials,
-                                                   E->net ? E->d_vol1d : nullptr, g->d_out);
+        if (E->net) HIS_CK(cudaStreamWaitEvent(s_main, join, 0));
+        eng_post_kernel<R><<<mc, 32, 0, s_main>>>(E->d_em, g->d_params, grids, g->c, g->d_partials,
+                                                  E->net ? E->d_vol1d : nullptr, g->d_out, m0);
         HIS_CK(cudaGetLastError());
     }
     return HIS_OK;
 }
 
 template <class R>
-int engine_enqueue_impl(his_engine* E, int n_steps) {
+int engine_enqueue_impl(his_engine* E, int chain, int n_steps) {
     his_grid* g = E->grid;
-    HIS_NT_DISPATCH(eng_enqueue_nt, R, g, E, n_steps);
+    HIS_NT_DISPATCH(eng_enqueue_nt, R, g, E, chain, n_steps);
 }
 
 template <class R>
@@ -241,12 +250,12 @@ int eng_profile_nt(his_grid* g, his_engine* E, int n_steps, double* ms) {
     for (int k = 0; k < n_steps && rc == HIS_OK; ++k) {
         cudaEventRecord(ev[0], E->s0);
         eng_pre_kernel<R><<<E->n, ENG_PRE_THREADS, E->pre_smem, E->s0>>>(E->d_em, g->d_params, grids, nets, links, g->c,
-                                                             E->d_netf, E->max_sub, exch);
+                                                             E->d_netf, E->max_sub, exch, 0);
         cudaEventRecord(ev[1], E->s0);
         if (E->net) {
             cudaStreamWaitEvent(E->s1, ev[1], 0);
             cudaEventRecord(ev[4], E->s1);
-            rc = net_engine_launch(E, E->s1);
+            rc = net_engine_launch(E, E->s1, 0, E->n);
             cudaEventRecord(ev[5], E->s1);
         }
         if (g->c.order == 2) {
@@ -264,7 +273,7 @@ int eng_profile_nt(his_grid* g, his_engine* E, int n_steps, double* ms) {
         cudaEventRecord(ev[3], E->s0);
         if (E->net) cudaStreamWaitEvent(E->s0, ev[5], 0);
         eng_post_kernel<R><<<E->n, 32, 0, E->s0>>>(E->d_em, g->d_params, grids, g->c, g->d_partials,
-                                                   E->net ? E->d_vol1d : nullptr, g->d_out);
+                                                   E->net ? E->d_vol1d : nullptr, g->d_out, 0);
         cudaEventRecord(ev[6], E->s0);
         cudaError_t ce = cudaEventSynchronize(ev[6]);
         if (ce != cudaSuccess) { rc = cuda_fail(ce, "his_engine_profile"); break; }
