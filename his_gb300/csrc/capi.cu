@@ -643,27 +643,70 @@ int32_t his_links_exchanged(his_links* L, double* totals, int32_t reset, void* s
 }  // extern "C"
 
 // ------------------------------------------------------------------------ engine
+// Split the members into n chains at the member boundaries nearest to equal shares of
+// the tiles (every chain at least one member); streams and events are created on
+// first use, and captured graphs are dropped so that the next advance recaptures.
+static int engine_split(his_engine* E, int n) {
+    his_grid* g = E->grid;
+    n = std::max(1, std::min(n, std::min(E->n, (int)his_engine::MAX_CHAINS)));
+    for (int c = 1; c < n; ++c) {
+        cudaError_t e = cudaSuccess;
+        if (!E->cs_main[c - 1]) e = cudaStreamCreateWithFlags(&E->cs_main[c - 1], cudaStreamNonBlocking);
+        if (e == cudaSuccess && !E->cs_side[c - 1])
+            e = cudaStreamCreateWithFlags(&E->cs_side[c - 1], cudaStreamNonBlocking);
+        for (cudaEvent_t* ev : {&E->cev_fork[c - 1], &E->cev_join[c - 1], &E->cev_out[c - 1]})
+            if (e == cudaSuccess && !*ev) e = cudaEventCreateWithFlags(ev, cudaEventDisableTiming);
+        if (e != cudaSuccess) return cuda_fail(e, "engine chains: streams and events");
+    }
+    for (int c = 0; c < his_engine::MAX_CHAINS; ++c) {
+        cudaGraphExec_t& x = E->exec_of(c);
+        if (x) cudaGraphExecDestroy(x);
+        x = nullptr;
+    }
+    E->n_chains = n;
+    E->chain_m[0] = 0;
+    E->chain_t[0] = 0;
+    int m = 0;
+    for (int c = 1; c < n; ++c) {
+        const long long want = (long long)g->n_tiles * c / n;
+        m = std::max(m + 1, 1);
+        while (m < E->n - (n - c) && g->tile0[m] < want) ++m;
+        E->chain_m[c] = m;
+        E->chain_t[c] = g->tile0[m];
+    }
+    E->chain_m[n] = E->n;
+    E->chain_t[n] = g->n_tiles;
+    return HIS_OK;
+}
+
 extern "C" {
 
 int32_t his_engine_destroy(his_engine* E) {
     if (!E) return HIS_OK;
     if (E->s0) cudaStreamSynchronize(E->s0);
     if (E->s1) cudaStreamSynchronize(E->s1);
-    for (cudaStream_t s : E->cs)
-        if (s) cudaStreamSynchronize(s);
+    for (int c = 0; c < his_engine::MAX_CHAINS - 1; ++c) {
+        if (E->cs_main[c]) cudaStreamSynchronize(E->cs_main[c]);
+        if (E->cs_side[c]) cudaStreamSynchronize(E->cs_side[c]);
+    }
     if (E->exec) cudaGraphExecDestroy(E->exec);
-    if (E->cexec) cudaGraphExecDestroy(E->cexec);
+    for (cudaGraphExec_t x : E->cexec)
+        if (x) cudaGraphExecDestroy(x);
     cudaFree(E->d_em);
     cudaFree(E->d_arena);
     cudaFree(E->d_netf);
     cudaFree(E->d_vol1d);
     if (E->h_em) cudaFreeHost(E->h_em);
-    for (cudaEvent_t ev : {E->ev_fork, E->ev_join, E->ev_in, E->ev_out, E->cev_fork, E->cev_join, E->cev_out})
+    for (cudaEvent_t ev : {E->ev_fork, E->ev_join, E->ev_in, E->ev_out})
         if (ev) cudaEventDestroy(ev);
+    for (int c = 0; c < his_engine::MAX_CHAINS - 1; ++c) {
+        for (cudaEvent_t ev : {E->cev_fork[c], E->cev_join[c], E->cev_out[c]})
+            if (ev) cudaEventDestroy(ev);
+        if (E->cs_main[c]) cudaStreamDestroy(E->cs_main[c]);
+        if (E->cs_side[c]) cudaStreamDestroy(E->cs_side[c]);
+    }
     if (E->s0) cudaStreamDestroy(E->s0);
     if (E->s1) cudaStreamDestroy(E->s1);
-    for (cudaStream_t s : E->cs)
-        if (s) cudaStreamDestroy(s);
     delete E;
     return HIS_OK;
 }
@@ -747,22 +790,14 @@ int32_t his_engine_create(his_grid* grid, his_net* net, his_links* links, int32_
     if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&E->s1, cudaStreamNonBlocking);
     for (cudaEvent_t* ev : {&E->ev_fork, &E->ev_join, &E->ev_in, &E->ev_out})
         if (e == cudaSuccess) e = cudaEventCreateWithFlags(ev, cudaEventDisableTiming);
-    // two chains split where the tiles are halved (at least one member each)
-    E->n_chains = n_members >= 2 ? 2 : 1;
-    if (E->n_chains == 2) {
-        int mid = 1;
-        while (mid < n_members - 1 && grid->tile0[mid] < grid->n_tiles / 2) ++mid;
-        E->chain_m[0] = 0; E->chain_m[1] = mid; E->chain_m[2] = n_members;
-        E->chain_t[0] = 0; E->chain_t[1] = grid->tile0[mid]; E->chain_t[2] = grid->n_tiles;
-        for (cudaStream_t& s : E->cs)
-            if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking);
-        for (cudaEvent_t* ev : {&E->cev_fork, &E->cev_join, &E->cev_out})
-            if (e == cudaSuccess) e = cudaEventCreateWithFlags(ev, cudaEventDisableTiming);
-    } else {
-        E->chain_m[0] = 0; E->chain_m[1] = E->chain_m[2] = n_members;
-        E->chain_t[0] = 0; E->chain_t[1] = E->chain_t[2] = grid->n_tiles;
-    }
     if (e != cudaSuccess) return fail(e, "his_engine_create: allocation");
+    // one chain per 512 tiles, at most 8: enough 2-D work per chain to hide another
+    // chain's per-step kernels, without splitting small batches into launch-bound slivers
+    int rc0 = engine_split(E, std::max(1, std::min(his_engine::MAX_CHAINS, grid->n_tiles / 512)));
+    if (rc0) {
+        his_engine_destroy(E);
+        return rc0;
+    }
     int rc = net_engine_prepare(E);
     if (rc == HIS_OK) rc = grid->prec == HIS_PREC_F64 ? engine_take_rate_f64(E) : engine_take_rate_f32(E);
     if (rc == HIS_OK) {
@@ -777,13 +812,14 @@ int32_t his_engine_create(his_grid* grid, his_net* net, his_links* links, int32_
     return HIS_OK;
 }
 
+
 static int engine_enqueue(his_engine* E, int chain, int n) {
     return E->grid->prec == HIS_PREC_F64 ? engine_enqueue_f64(E, chain, n) : engine_enqueue_f32(E, chain, n);
 }
 
 // One graph of graph_steps steps of one chain, captured from the chain's main stream.
 static int engine_capture(his_engine* E, int chain, cudaGraphExec_t* exec) {
-    cudaStream_t s = chain == 0 ? E->s0 : E->cs[0];
+    cudaStream_t s = E->main_of(chain);
     cudaGraph_t graph = nullptr;
     HIS_CK(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
     int rc = engine_enqueue(E, chain, E->graph_steps);
@@ -800,37 +836,43 @@ int32_t his_engine_advance(his_engine* E, int32_t n_steps, void* stream) {
     if (!E) return bad("engine is NULL");
     if (n_steps < 0) return bad("n_steps must be >= 0");
     cudaStream_t caller = (cudaStream_t)stream;
-    const bool two = E->n_chains == 2;
+    const int nc = E->n_chains;
     HIS_CK(cudaEventRecord(E->ev_in, caller));
-    HIS_CK(cudaStreamWaitEvent(E->s0, E->ev_in, 0));
-    if (two) HIS_CK(cudaStreamWaitEvent(E->cs[0], E->ev_in, 0));
+    for (int c = 0; c < nc; ++c) HIS_CK(cudaStreamWaitEvent(E->main_of(c), E->ev_in, 0));
     if (!E->exec && n_steps >= E->graph_steps) {
-        int rc = engine_capture(E, 0, &E->exec);
-        if (rc == HIS_OK && two) rc = engine_capture(E, 1, &E->cexec);
-        if (rc) return rc;
+        for (int c = 0; c < nc; ++c) {
+            int rc = engine_capture(E, c, &E->exec_of(c));
+            if (rc) return rc;
+        }
     }
     // the chains run independently until the end of the call, each launching its
     // graphs back to back on its own stream, so their relative phase is kept
     int done = 0;
     if (E->exec) {
-        for (; done + E->graph_steps <= n_steps; done += E->graph_steps) {
-            HIS_CK(cudaGraphLaunch(E->exec, E->s0));
-            if (two) HIS_CK(cudaGraphLaunch(E->cexec, E->cs[0]));
-        }
+        for (; done + E->graph_steps <= n_steps; done += E->graph_steps)
+            for (int c = 0; c < nc; ++c) HIS_CK(cudaGraphLaunch(E->exec_of(c), E->main_of(c)));
     }
     if (done < n_steps) {
-        int rc = engine_enqueue(E, 0, n_steps - done);
-        if (rc == HIS_OK && two) rc = engine_enqueue(E, 1, n_steps - done);
-        if (rc) return rc;
+        for (int c = 0; c < nc; ++c) {
+            int rc = engine_enqueue(E, c, n_steps - done);
+            if (rc) return rc;
+        }
     }
-    HIS_CK(cudaEventRecord(E->ev_out, E->s0));
-    HIS_CK(cudaStreamWaitEvent(caller, E->ev_out, 0));
-    if (two) {
-        HIS_CK(cudaEventRecord(E->cev_out, E->cs[0]));
-        HIS_CK(cudaStreamWaitEvent(caller, E->cev_out, 0));
+    for (int c = 0; c < nc; ++c) {
+        HIS_CK(cudaEventRecord(E->out_of(c), E->main_of(c)));
+        HIS_CK(cudaStreamWaitEvent(caller, E->out_of(c), 0));
     }
     return HIS_OK;
 }
+
+int32_t his_engine_set_chains(his_engine* E, int32_t n_chains) {
+    if (!E) return bad("engine is NULL");
+    if (n_chains < 1 || n_chains > his_engine::MAX_CHAINS) return bad("n_chains must be in [1, 8]");
+    for (int c = 0; c < E->n_chains; ++c) HIS_CK(cudaStreamSynchronize(E->main_of(c)));
+    return engine_split(E, n_chains);
+}
+
+int32_t his_engine_chains(const his_engine* E) { return E ? E->n_chains : 0; }
 
 int32_t his_engine_report(his_engine* E, his_member_report* reports, void* stream) {
     if (!E || !reports) return bad("engine and reports are required");

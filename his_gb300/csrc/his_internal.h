@@ -83,13 +83,21 @@ struct his_engine {
     cudaGraphExec_t exec = nullptr;
     // The members run as n_chains independent chains (members [chain_m[c], chain_m[c+1]),
     // tiles [chain_t[c], chain_t[c+1])), each with its own streams and graph, so one
-    // chain's latency-bound pre/post kernels overlap the other's 2-D stages.  Chain 0
-    // uses s0/s1 and the events above; chain 1 uses cs[0]/cs[1] and cev[].
+    // chain's latency-bound pre/post kernels overlap another's 2-D stages.  Chain 0
+    // uses s0/s1, ev_fork/ev_join/ev_out and exec; chain c >= 1 the entries c - 1 of
+    // the arrays below.
+    static constexpr int MAX_CHAINS = 8;
     int n_chains = 1;
-    int chain_m[3] = {0, 0, 0}, chain_t[3] = {0, 0, 0};
-    cudaStream_t cs[2] = {nullptr, nullptr};
-    cudaEvent_t cev_fork = nullptr, cev_join = nullptr, cev_out = nullptr;
-    cudaGraphExec_t cexec = nullptr;
+    int chain_m[MAX_CHAINS + 1] = {}, chain_t[MAX_CHAINS + 1] = {};
+    cudaStream_t cs_main[MAX_CHAINS - 1] = {}, cs_side[MAX_CHAINS - 1] = {};
+    cudaEvent_t cev_fork[MAX_CHAINS - 1] = {}, cev_join[MAX_CHAINS - 1] = {}, cev_out[MAX_CHAINS - 1] = {};
+    cudaGraphExec_t cexec[MAX_CHAINS - 1] = {};
+    cudaStream_t main_of(int c) const { return c == 0 ? s0 : cs_main[c - 1]; }
+    cudaStream_t side_of(int c) const { return c == 0 ? s1 : cs_side[c - 1]; }
+    cudaEvent_t fork_of(int c) const { return c == 0 ? ev_fork : cev_fork[c - 1]; }
+    cudaEvent_t join_of(int c) const { return c == 0 ? ev_join : cev_join[c - 1]; }
+    cudaEvent_t out_of(int c) const { return c == 0 ? ev_out : cev_out[c - 1]; }
+    cudaGraphExec_t& exec_of(int c) { return c == 0 ? exec : cexec[c - 1]; }
 };
 
 namespace his {

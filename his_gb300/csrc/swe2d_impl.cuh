@@ -192,8 +192,8 @@ int eng_enqueue_nt(his_grid* g, his_engine* E, int chain, int n_steps) {
     double* exch = E->links ? E->links->d_exch : nullptr;
     const int m0 = E->chain_m[chain], mc = E->chain_m[chain + 1] - m0;
     const int t0 = E->chain_t[chain], tc = E->chain_t[chain + 1] - t0;
-    cudaStream_t s_main = chain == 0 ? E->s0 : E->cs[0], s_side = chain == 0 ? E->s1 : E->cs[1];
-    cudaEvent_t fork = chain == 0 ? E->ev_fork : E->cev_fork, join = chain == 0 ? E->ev_join : E->cev_join;
+    cudaStream_t s_main = E->main_of(chain), s_side = E->side_of(chain);
+    cudaEvent_t fork = E->fork_of(chain), join = E->join_of(chain);
     if (mc == 0) return HIS_OK;
     for (int k = 0; k < n_steps; ++k) {
         eng_pre_kernel<R><<<mc, ENG_PRE_THREADS, E->pre_smem, s_main>>>(E->d_em, g->d_params, grids, nets, links, g->c,

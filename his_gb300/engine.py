@@ -270,13 +270,15 @@ class Member:
 class FloodEngine:
     def __init__(self, storms: list, cfg: SolverConfig | None = None, precision: str = "fp32",
                  device=None, tile="auto", graph_steps: int = 16, max_sub: int = 64, couple: bool = True,
-                 track_peaks: bool = False, output_interval: float | None = None):
+                 track_peaks: bool = False, output_interval: float | None = None, chains: int | None = None):
         """storms: Storm objects (new members) or Member objects (members moved from
         another engine, resumed from their records).  tile: (tile_x, tile_y) strip width
         and chunk height of the 2-D kernels, (0, 0) or None for the defaults, "auto"
         (default) to let the autotuner measure the candidates for this batch (cached per
         device, precision and batch shape).  output_interval: seconds between the
-        outputs of new members (None: no series; running peaks with track_peaks)."""
+        outputs of new members (None: no series; running peaks with track_peaks).
+        chains: independent member chains the device advances side by side (1..8;
+        None: the library's default, one per 512 strip-chunk tiles)."""
         if not storms:
             raise ValueError("FloodEngine needs at least one storm")
         self.cfg = cfg or SolverConfig()
@@ -336,6 +338,8 @@ class FloodEngine:
                                                    self._links if self.coupled else None, self.B, fdesc,
                                                    int(max_sub), int(graph_steps), C.byref(self._engine)),
                        "his_engine_create")
+            if chains is not None:
+                _lib.check(self._lib.his_engine_set_chains(self._engine, int(chains)), "his_engine_set_chains")
             if any(m.record is not None for m in members):
                 reps = (_lib.MemberReport * self.B)()
                 mask = np.zeros(self.B, dtype=np.int32)
@@ -379,6 +383,11 @@ class FloodEngine:
 
     def __del__(self):
         self.close()
+
+    @property
+    def chains(self) -> int:
+        """Independent member chains the device advances side by side."""
+        return int(self._lib.his_engine_chains(self._engine))
 
     def close(self) -> None:
         """Free the engine's device tables (the members keep their state)."""

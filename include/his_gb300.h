@@ -280,8 +280,21 @@ int32_t his_engine_create(his_grid* grid, his_net* net, his_links* links, int32_
                           const his_forcing_desc* forcing, int32_t max_sub, int32_t graph_steps, his_engine** out);
 int32_t his_engine_destroy(his_engine* engine);
 
-/* Enqueue n_steps steps of every running member on `stream` (asynchronous). */
+/* Enqueue n_steps steps of every running member on `stream` (asynchronous).  The
+ * members run as independent chains (his_engine_set_chains), each on its own streams
+ * and graphs; they join `stream` at the end of the call. */
 int32_t his_engine_advance(his_engine* engine, int32_t n_steps, void* stream);
+
+/* Split the members into n_chains (1..8, at most one per member) independent chains
+ * of about equal 2-D work, each advanced on its own streams and CUDA graphs, so that
+ * one chain's latency-bound per-step kernels (dt, exchange, forcing, accounting)
+ * overlap another's 2-D stages.  Results do not depend on the split (every member's
+ * arithmetic is the same).  Default at creation: one chain per 512 strip-chunk tiles,
+ * between 1 and 8 (64 members of 400 x 325 cells: 8).  Waits for the engine's streams;
+ * graphs are recaptured by the next advance.
+ * No reference counterpart (the reference steps one batch with one shared dt). */
+int32_t his_engine_set_chains(his_engine* engine, int32_t n_chains);
+int32_t his_engine_chains(const his_engine* engine);
 
 /* Per-member reports (host out, n_members; synchronises). */
 int32_t his_engine_report(his_engine* engine, his_member_report* reports, void* stream);
