@@ -109,6 +109,7 @@ SIGNATURES = {
     "his_engine_advance": (C.c_int32, [_H, C.c_int32, C.c_void_p]),
     "his_engine_set_chains": (C.c_int32, [_H, C.c_int32]),
     "his_engine_chains": (C.c_int32, [_H]),
+    "his_engine_default_chains": (C.c_int32, [C.c_int32, C.c_int32]),
     "his_engine_report": (C.c_int32, [_H, C.POINTER(MemberReport), C.c_void_p]),
     "his_engine_resume": (C.c_int32, [_H, C.POINTER(MemberReport), _I32P, C.c_void_p]),
     "his_engine_profile": (C.c_int32, [_H, C.c_int32, _F64P, C.c_void_p]),

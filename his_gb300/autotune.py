@@ -7,10 +7,13 @@ grid sizes, the batch and the precision: narrow strips recompute more halo
 columns, short chunks more halo rows, and the number of strip-chunks decides how
 evenly the CTAs fill the GPU (152 SMs, 14 resident 64-thread CTAs each in float32).
 
-``choose_tile`` times ``his_grid_step`` for every candidate on throw-away copies of
-the members' state (the fields are shared read-only), keeps the fastest and caches
-the choice per device, precision, spatial order and batch shape, in memory and in a
-JSON file (``$HIS_GB300_TUNE_CACHE``, default ``~/.cache/his_gb300/tiles.json``).
+``choose_tile`` times every candidate the way the engine runs it: the members split
+into that decomposition's default number of chains (``his_engine_default_chains``,
+at tile-balanced member boundaries), one grid set per chain stepped on its own
+stream, all side by side.  It works on throw-away copies of the members' state (the
+fields are shared read-only), keeps the fastest and caches the choice per device,
+precision, spatial order and batch shape, in memory and in a JSON file
+(``$HIS_GB300_TUNE_CACHE``, default ``~/.cache/his_gb300/tiles.json``).
 
 The decomposition changes only the order in which the volume partials are summed
 (in the compute type within a strip-chunk, in float64 across them), never a cell's
@@ -97,12 +100,44 @@ def candidates(shapes: list[tuple[int, int]]) -> list[tuple[int, int]]:
     return out
 
 
-def _time_steps(lib, g, params, stream, steps) -> float:
+def tiles_per_member(shapes: list[tuple[int, int]], tile: tuple[int, int]) -> list[int]:
+    """Strip-chunks of each member for a decomposition (his_grid_create's split)."""
+    tx, ty = tile
+    return [(-(-nx // tx)) * (-(-ny // ty)) for ny, nx in shapes]
+
+
+def chain_bounds(counts: list[int], k: int) -> list[int]:
+    """Member boundaries of k chains at the nearest shares of the tiles, every chain
+    at least one member (the engine's split)."""
+    n = len(counts)
+    tile0 = np.concatenate([[0], np.cumsum(counts)]).astype(np.int64)
+    total = int(tile0[-1])
+    bounds, m = [0], 0
+    for c in range(1, k):
+        want = total * c // k
+        m = max(m + 1, 1)
+        while m < n - (k - c) and tile0[m] < want:
+            m += 1
+        bounds.append(m)
+    bounds.append(n)
+    return bounds
+
+
+def _time_chained(lib, sets, streams, main, steps) -> float:
+    """Mean device time of one step of every grid set, the sets side by side on
+    their own streams."""
     e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-    e0.record(stream)
+    e0.record(main)
+    for s in streams[:len(sets)]:
+        s.wait_event(e0)
     for _ in range(steps):
-        _lib.check(lib.his_grid_step(g, params, None, stream.cuda_stream), "his_grid_step")
-    e1.record(stream)
+        for (g, params), s in zip(sets, streams):
+            _lib.check(lib.his_grid_step_async(g, params, None, s.cuda_stream), "his_grid_step_async")
+    for s in streams[:len(sets)]:
+        ev = torch.cuda.Event()
+        ev.record(s)
+        main.wait_event(ev)
+    e1.record(main)
     e1.synchronize()
     return e0.elapsed_time(e1) / steps
 
@@ -150,24 +185,34 @@ def choose_tile(device: torch.device, prec: int, cfg, descs, states: list[list[t
                 params[b].t = 0.0
                 params[b].rain = 1e-5
             cands = candidates(shapes)
-            grids = {}
+            streams = [torch.cuda.Stream(device) for _ in range(8)]
+            sets = {}
             try:
                 for tile in cands:
-                    g = C.c_void_p()
-                    _lib.check(lib.his_grid_create(prec, C.byref(cfgc), n, tdesc, tile[0], tile[1], C.byref(g)),
-                               "his_grid_create")
-                    grids[tile] = g
+                    counts = tiles_per_member(shapes, tile)
+                    k = int(lib.his_engine_default_chains(n, sum(counts)))
+                    bounds = chain_bounds(counts, k)
+                    sets[tile] = []
+                    for b0, b1 in zip(bounds[:-1], bounds[1:]):
+                        sub_desc = (_lib.GridDesc * (b1 - b0))(*[tdesc[b] for b in range(b0, b1)])
+                        sub_par = (_lib.StepParams * (b1 - b0))(*[params[b] for b in range(b0, b1)])
+                        g = C.c_void_p()
+                        _lib.check(lib.his_grid_create(prec, C.byref(cfgc), b1 - b0, sub_desc, tile[0], tile[1],
+                                                       C.byref(g)), "his_grid_create")
+                        sets[tile].append((g, sub_par))
                 # warm up on the first candidate until the clocks have settled
-                first = grids[cands[0]]
-                per = _time_steps(lib, first, params, stream, 1)
-                _time_steps(lib, first, params, stream, max(1, int(WARMUP_MS / max(per, 1e-3))))
+                first = sets[cands[0]]
+                per = _time_chained(lib, first, streams, stream, 1)
+                _time_chained(lib, first, streams, stream, max(1, int(WARMUP_MS / max(per, 1e-3))))
                 best = {tile: float("inf") for tile in cands}
                 for _ in range(ROUNDS):                      # interleaved rounds, best per candidate
                     for tile in cands:
-                        best[tile] = min(best[tile], _time_steps(lib, grids[tile], params, stream, TIMED_STEPS))
+                        best[tile] = min(best[tile], _time_chained(lib, sets[tile], streams, stream, TIMED_STEPS))
             finally:
-                for g in grids.values():
-                    lib.his_grid_destroy(g)
+                torch.cuda.synchronize(device)
+                for grid_sets in sets.values():
+                    for g, _ in grid_sets:
+                        lib.his_grid_destroy(g)
             times = {f"{tx}x{ty}": ms for (tx, ty), ms in best.items()}
         del copies
         best = min(times, key=times.get)
@@ -178,4 +223,4 @@ def choose_tile(device: torch.device, prec: int, cfg, descs, states: list[list[t
         return tile
 
 
-__all__ = ["choose_tile", "candidates", "tune_key", "cache_path"]
+__all__ = ["choose_tile", "candidates", "tune_key", "cache_path", "tiles_per_member", "chain_bounds"]

@@ -646,6 +646,8 @@ int32_t his_links_exchanged(his_links* L, double* totals, int32_t reset, void* s
 // Split the members into n chains at the member boundaries nearest to equal shares of
 // the tiles (every chain at least one member); streams and events are created on
 // first use, and captured graphs are dropped so that the next advance recaptures.
+extern "C" int32_t his_engine_default_chains(int32_t n_members, int32_t n_tiles);
+
 static int engine_split(his_engine* E, int n) {
     his_grid* g = E->grid;
     n = std::max(1, std::min(n, std::min(E->n, (int)his_engine::MAX_CHAINS)));
@@ -791,9 +793,7 @@ int32_t his_engine_create(his_grid* grid, his_net* net, his_links* links, int32_
     for (cudaEvent_t* ev : {&E->ev_fork, &E->ev_join, &E->ev_in, &E->ev_out})
         if (e == cudaSuccess) e = cudaEventCreateWithFlags(ev, cudaEventDisableTiming);
     if (e != cudaSuccess) return fail(e, "his_engine_create: allocation");
-    // one chain per 512 tiles, at most 8: enough 2-D work per chain to hide another
-    // chain's per-step kernels, without splitting small batches into launch-bound slivers
-    int rc0 = engine_split(E, std::max(1, std::min(his_engine::MAX_CHAINS, grid->n_tiles / 512)));
+    int rc0 = engine_split(E, his_engine_default_chains(n_members, grid->n_tiles));
     if (rc0) {
         his_engine_destroy(E);
         return rc0;
@@ -873,6 +873,13 @@ int32_t his_engine_set_chains(his_engine* E, int32_t n_chains) {
 }
 
 int32_t his_engine_chains(const his_engine* E) { return E ? E->n_chains : 0; }
+
+// one chain per 256 strip-chunk tiles, at most 8 and at most one per member: enough
+// 2-D work per chain to hide another chain's per-step kernels, without splitting
+// small batches into launch-bound slivers
+int32_t his_engine_default_chains(int32_t n_members, int32_t n_tiles) {
+    return std::max(1, std::min(std::min((int)his_engine::MAX_CHAINS, (int)n_members), (int)(n_tiles / 256)));
+}
 
 int32_t his_engine_report(his_engine* E, his_member_report* reports, void* stream) {
     if (!E || !reports) return bad("engine and reports are required");

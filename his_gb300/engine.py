@@ -278,7 +278,7 @@ class FloodEngine:
         device, precision and batch shape).  output_interval: seconds between the
         outputs of new members (None: no series; running peaks with track_peaks).
         chains: independent member chains the device advances side by side (1..8;
-        None: the library's default, one per 512 strip-chunk tiles)."""
+        None: the library's default, one per 256 strip-chunk tiles)."""
         if not storms:
             raise ValueError("FloodEngine needs at least one storm")
         self.cfg = cfg or SolverConfig()

@@ -289,12 +289,15 @@ int32_t his_engine_advance(his_engine* engine, int32_t n_steps, void* stream);
  * of about equal 2-D work, each advanced on its own streams and CUDA graphs, so that
  * one chain's latency-bound per-step kernels (dt, exchange, forcing, accounting)
  * overlap another's 2-D stages.  Results do not depend on the split (every member's
- * arithmetic is the same).  Default at creation: one chain per 512 strip-chunk tiles,
- * between 1 and 8 (64 members of 400 x 325 cells: 8).  Waits for the engine's streams;
- * graphs are recaptured by the next advance.
+ * arithmetic is the same).  Default at creation: his_engine_default_chains (64 members
+ * of 400 x 325 cells in 58 x 48 tiles: 8).  Waits for the engine's streams; graphs are
+ * recaptured by the next advance.
  * No reference counterpart (the reference steps one batch with one shared dt). */
 int32_t his_engine_set_chains(his_engine* engine, int32_t n_chains);
 int32_t his_engine_chains(const his_engine* engine);
+/* The default chain count for n_members members in n_tiles strip-chunk tiles: one per
+ * 256 tiles, at least 1, at most 8 and at most n_members. */
+int32_t his_engine_default_chains(int32_t n_members, int32_t n_tiles);
 
 /* Per-member reports (host out, n_members; synchronises). */
 int32_t his_engine_report(his_engine* engine, his_member_report* reports, void* stream);

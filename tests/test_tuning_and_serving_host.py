@@ -51,3 +51,22 @@ def test_request_stream_is_seeded():
     t = np.array([x[0] for x in a])
     assert np.all(np.diff(t) > 0) and t[-1] <= 30.0
     assert {x[1] for x in a} <= {0, 1, 2}
+
+
+def test_chain_split_matches_the_engine_rule():
+    """Tiles per member follow his_grid_create's split (77 strip-chunks of a 400 x 325
+    grid at 58 x 32), and chain bounds give every chain at least one member at the
+    nearest tile shares."""
+    from his_gb300.autotune import chain_bounds, tiles_per_member
+    assert tiles_per_member([(325, 400)], (58, 32)) == [77]
+    assert tiles_per_member([(81, 100), (163, 200)], (58, 48)) == [4, 16]
+    counts = [77] * 64
+    assert chain_bounds(counts, 8) == [0, 8, 16, 24, 32, 40, 48, 56, 64]
+    assert chain_bounds(counts, 1) == [0, 64]
+    uneven = [4] * 16 + [16] * 16 + [56] * 16
+    b = chain_bounds(uneven, 4)
+    assert b[0] == 0 and b[-1] == 48 and all(x < y for x, y in zip(b[:-1], b[1:]))
+    tot = sum(uneven)
+    shares = [sum(uneven[x:y]) for x, y in zip(b[:-1], b[1:])]
+    assert max(shares) <= tot / 4 + 56
+    assert chain_bounds([5, 1, 1], 3) == [0, 1, 2, 3]
