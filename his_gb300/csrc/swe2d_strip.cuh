@@ -47,11 +47,14 @@ struct StripGeom {
     static_assert((size_t)4 * RING * NT >= (size_t)32 * NRED, "reduction scratch must fit in the cell ring");
     static constexpr size_t smem_bytes = sizeof(Q4<R>) * quads + sizeof(R) * th;
     // resident CTAs per SM the float32 kernels are register-capped for (shared memory
-    // allows 14 of 64 threads): about 896 threads' worth for stage 1 and 768 for the
-    // larger stage-2 body, so that it keeps its live values in registers; float64 keeps
-    // the compiler's choice (one CTA of any width must fit the register file)
+    // allows 14 of 64 threads): about 768 threads' worth for stage 1 and 640 for the
+    // larger stage-2 body, so that they keep their live values in registers.  With the
+    // engine's member chains running side by side this beat tighter caps (896 / 768:
+    // 0.474 against 0.466 ms per step at 64 x 400 x 325) and looser ones (640 / 512:
+    // 0.502 ms).  float64 keeps the compiler's choice (one CTA of any width must fit
+    // the register file)
     static constexpr int min_ctas(int stage) {
-        return sizeof(R) == 4 ? ((stage == 1 ? 896 : 768) / NT > 0 ? (stage == 1 ? 896 : 768) / NT : 1) : 1;
+        return sizeof(R) == 4 ? ((stage == 1 ? 768 : 640) / NT > 0 ? (stage == 1 ? 768 : 640) / NT : 1) : 1;
     }
 };
 
