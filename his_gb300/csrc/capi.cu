@@ -207,6 +207,14 @@ int32_t his_grid_destroy(his_grid* g) {
     cudaFree(g->d_scratch);
     if (g->h_out) cudaFreeHost(g->h_out);
     stage_free(g->params_stage);
+    for (int k = 0; k < his_grid::MAX_PARTS - 1; ++k) {
+        if (g->ps[k]) {
+            cudaStreamSynchronize(g->ps[k]);
+            cudaStreamDestroy(g->ps[k]);
+        }
+        if (g->pev_join[k]) cudaEventDestroy(g->pev_join[k]);
+    }
+    if (g->pev_fork) cudaEventDestroy(g->pev_fork);
     delete g;
     return HIS_OK;
 }
@@ -217,6 +225,33 @@ int64_t his_grid_scratch_bytes(const his_grid* g) {
 
 // Every field is set: the snapshot pointers and slot are NULL / -1 (the drop-in step
 // writes no output series), which the kernels read to decide whether to write one.
+extern "C" int32_t his_engine_default_chains(int32_t n_members, int32_t n_tiles);
+
+// Parts of a grid step's stage launches (his_grid::n_parts): the engine's chain rule,
+// cut at the member boundaries nearest to equal shares of the tiles; the streams and
+// events are created here, on the first step.
+static int grid_parts_setup(his_grid* g) {
+    const int np = std::min((int)his_grid::MAX_PARTS, (int)his_engine_default_chains(g->n, g->n_tiles));
+    cudaError_t e = cudaSuccess;
+    if (np > 1) e = cudaEventCreateWithFlags(&g->pev_fork, cudaEventDisableTiming);
+    for (int k = 0; k + 1 < np && e == cudaSuccess; ++k) {
+        e = cudaStreamCreateWithFlags(&g->ps[k], cudaStreamNonBlocking);
+        if (e == cudaSuccess) e = cudaEventCreateWithFlags(&g->pev_join[k], cudaEventDisableTiming);
+    }
+    if (e != cudaSuccess) return cuda_fail(e, "grid step: part streams");
+    g->part_t[0] = 0;
+    int m = 0;
+    for (int k = 1; k < np; ++k) {
+        const long long want = (long long)g->n_tiles * k / np;
+        m = std::max(m + 1, 1);
+        while (m < g->n - (np - k) && g->tile0[m] < want) ++m;
+        g->part_t[k] = g->tile0[m];
+    }
+    g->part_t[np] = g->n_tiles;
+    g->n_parts = np;
+    return HIS_OK;
+}
+
 static int fill_params(his_grid* g, const his_step_params* p, StepParams* sp) {
     for (int m = 0; m < g->n; ++m) {
         const his_step_params& q = p[m];
@@ -259,6 +294,10 @@ static int fetch_out(his_grid* g, cudaStream_t s) {
 
 int32_t his_grid_step(his_grid* g, const his_step_params* params, double* vols, void* stream) {
     if (!g || !params) return bad("grid and params are required");
+    if (!g->n_parts) {
+        int rc = grid_parts_setup(g);
+        if (rc) return rc;
+    }
     cudaStream_t s = (cudaStream_t)stream;
     int rc = upload_params(g, params, s);
     if (rc) return rc;
@@ -272,6 +311,10 @@ int32_t his_grid_step(his_grid* g, const his_step_params* params, double* vols, 
 
 int32_t his_grid_step_async(his_grid* g, const his_step_params* params, double* vols, void* stream) {
     if (!g || !params) return bad("grid and params are required");
+    if (!g->n_parts) {
+        int rc = grid_parts_setup(g);
+        if (rc) return rc;
+    }
     bool direct = false;
     int rc = vols ? check_async_out(vols, "vols", &direct) : HIS_OK;
     if (rc) return rc;

@@ -38,6 +38,15 @@ struct his_grid {
     size_t scratch_bytes = 0;
     size_t table_bytes = 0;
     HostStage params_stage;                  // his_grid_step_async parameters
+    // The 2-D stages of a grid step run as n_parts launches over whole members' tiles
+    // [part_t[k], part_t[k + 1]), part 0 on the caller's stream and part k >= 1 on
+    // ps[k - 1], forked and joined with events, so that the parts fill each other's
+    // waves.  Set up on the first step (grid_parts_setup in capi.cu).
+    static constexpr int MAX_PARTS = 8;
+    int n_parts = 0;                         // 0: not set up yet
+    int part_t[MAX_PARTS + 1] = {};
+    cudaStream_t ps[MAX_PARTS - 1] = {};
+    cudaEvent_t pev_fork = nullptr, pev_join[MAX_PARTS - 1] = {};
 };
 
 struct his_net {

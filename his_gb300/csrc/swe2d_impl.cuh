@@ -43,9 +43,28 @@ int launch_stages(his_grid* g, cudaStream_t s, int t0 = 0, int count = -1) {
     return HIS_OK;
 }
 
+// The stages over all tiles in g->n_parts parts side by side (part 0 on s), joined
+// back into s.
+template <class R, int NT>
+int launch_stages_parted(his_grid* g, cudaStream_t s) {
+    const int np = g->n_parts;
+    if (np <= 1) return launch_stages<R, NT>(g, s);
+    HIS_CK(cudaEventRecord(g->pev_fork, s));
+    for (int k = 1; k < np; ++k) {
+        HIS_CK(cudaStreamWaitEvent(g->ps[k - 1], g->pev_fork, 0));
+        int rc = launch_stages<R, NT>(g, g->ps[k - 1], g->part_t[k], g->part_t[k + 1] - g->part_t[k]);
+        if (rc) return rc;
+        HIS_CK(cudaEventRecord(g->pev_join[k - 1], g->ps[k - 1]));
+    }
+    int rc = launch_stages<R, NT>(g, s, g->part_t[0], g->part_t[1] - g->part_t[0]);
+    if (rc) return rc;
+    for (int k = 1; k < np; ++k) HIS_CK(cudaStreamWaitEvent(s, g->pev_join[k - 1], 0));
+    return HIS_OK;
+}
+
 template <class R, int NT>
 int launch_step_nt(his_grid* g, cudaStream_t s, double* ext) {
-    int rc = launch_stages<R, NT>(g, s);
+    int rc = launch_stages_parted<R, NT>(g, s);
     if (rc) return rc;
     finalize_kernel<R><<<g->n, 32, 0, s>>>(reinterpret_cast<const Grid<R>*>(g->d_grids), g->d_params, g->c,
                                            g->d_partials, g->d_out, 0, ext);

@@ -92,6 +92,10 @@ int64_t his_grid_scratch_bytes(const his_grid* grid);
 /* Advance every member by one SSP-RK2 step with its own params (host array of
  * n_members).  If vols is non-NULL it receives n_members x 5 float64 volumes
  * (bnd_in, bnd_out, rain, infil, clip; m^3) and the call synchronises `stream`.
+ * Large sets run their stage launches as up to 8 parts of whole members on library
+ * streams forked from `stream` and joined back into it before the step's totals
+ * (his_engine_default_chains' rule), so the parts fill each other's waves; results
+ * do not depend on it.
  * Replaces hydrointel/solver/swe2d.py:298-371 (SWE2D.step / _step_core). */
 int32_t his_grid_step(his_grid* grid, const his_step_params* params, double* vols, void* stream);
 
