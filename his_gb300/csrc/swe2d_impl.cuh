@@ -184,7 +184,7 @@ template <class R>
 int exchange_impl(his_links* l, const Consts& c, double dt, cudaStream_t s) {
     if (l->smem > 48 * 1024)
         HIS_CK(cudaFuncSetAttribute(exchange_kernel<R>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)l->smem));
-    exchange_kernel<R><<<l->n, 256, l->smem, s>>>(l->d_links, l->net->d_nets,
+    exchange_kernel<R><<<l->n, EXCHANGE_THREADS, l->smem, s>>>(l->d_links, l->net->d_nets,
                                                   reinterpret_cast<const Grid<R>*>(l->grid->d_grids), c, dt, l->d_V,
                                                   l->d_exch);
     HIS_CK(cudaGetLastError());
