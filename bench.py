@@ -249,7 +249,7 @@ def serving_leg(window_s: float):
     latency is arrival to result."""
     from his_gb300.serving import FloodServer, request_stream
     reqs = request_stream(2.0, window_s)
-    srv = FloodServer(precision="fp32", chunk_steps=256, tile=(58, 48))
+    srv = FloodServer(precision="fp32", chunk_steps=256, tile=(58, 16))
     st = srv.serve(reqs, max_wall_s=window_s + 240.0)
     d = dict(st.__dict__)
     d["workload"] = (f"served: Poisson 2 req/s over {window_s:.0f} s, grids 100x81 @ 80 m / 200x163 @ 40 m / "
