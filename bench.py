@@ -13,7 +13,9 @@ Printed (rank 0, one JSON line): cell-steps/s (whole job), storms/hour of the
 batch and of the plain float64 single-storm engine at the same resolution, the
 end-to-end rate through the drop-in C-ABI path with host buffers, the roofline of
 the dominant kernel against the measured HBM peak, SM clocks sampled during the
-timed region, and the oracle's CPU float64 rate on this host as a baseline.
+timed region, the float32 form's error against float64 on the 100 x 81 storm (peak
+depth, arrival time, volume), and the oracle's CPU float64 rate on this host as a
+baseline.
 
 --impl reference times the CPU restatement of the reference's float64 step (the
 oracle, all host threads) on a bounded sample of the same workload.
@@ -257,6 +259,28 @@ def serving_leg(window_s: float):
     return d
 
 
+def accuracy_leg(interval_s: float = 60.0) -> dict:
+    """Error of the float32 production form against the plain float64 method on the
+    100x81 @ 80 m storm run to its end: peak depth, arrival time (first output at
+    0.1 m, outputs every interval_s) and volume (his_gb300.accuracy.compare)."""
+    from his_gb300 import workloads as W
+    from his_gb300.accuracy import compare
+    from his_gb300.config import SolverConfig
+    from his_gb300.engine import FloodEngine
+    storm = W.plain_small()
+    res = {}
+    for prec in ("fp64", "fp32"):
+        fe = FloodEngine([storm], SolverConfig(slot_width_frac=storm.slot_width_frac), precision=prec,
+                         track_peaks=True, output_interval=interval_s)
+        fe.run(chunk=512)
+        res[prec] = fe.flood_results()[0]
+        fe.close()
+    m = compare(res["fp32"], res["fp64"])
+    m["mass_error_fp32"] = float(res["fp32"].mass_balance_error)
+    m["workload"] = "100x81 @ 80 m coupled storm to its end, float32 production form against float64"
+    return m
+
+
 def e2e_dropin(storms, steps: int):
     """Same metric through the drop-in public API (batched CoupledEngine -> C ABI, host
     buffers): every step uploads its step parameters and 1-D forcing from host memory
@@ -373,6 +397,8 @@ def run_ours(args, world, rank, local):
         del pe
         torch.cuda.empty_cache()
         out["uneven_batch"] = uneven_leg(args.storm_seconds)
+        torch.cuda.empty_cache()
+        out["accuracy_c1"] = accuracy_leg()
         torch.cuda.empty_cache()
         if args.serve_seconds > 0:
             out["serving"] = serving_leg(args.serve_seconds)

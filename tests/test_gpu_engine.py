@@ -133,19 +133,22 @@ def test_full_storm_mass_balance(precision):
 def test_fp32_production_form_against_fp64():
     """Production form (float32 state and fluxes, float64 accumulators) against the plain
     float64 method on the same storm run to its end: peak-depth RMSE <= 1 cm, mass
-    error < 1e-3, and the volume error reported."""
+    error < 1e-3, flood arrival (first 60-s output at 0.1 m) within one output interval
+    in RMSE, and the volume error reported."""
     from his_gb300 import workloads as W
+    from his_gb300.accuracy import compare
     from his_gb300.config import SolverConfig
     from his_gb300.engine import FloodEngine
     storm = W.plain_small()
-    runs = {}
+    runs, floods = {}, {}
     for prec in ("fp64", "fp32"):
         fe = FloodEngine([storm], SolverConfig(slot_width_frac=storm.slot_width_frac), precision=prec,
-                         track_peaks=True)
+                         track_peaks=True, output_interval=60.0)
         reps = fe.run(chunk=512)
         assert reps[0].status == 1
         fe.assert_mass_ok()
         runs[prec] = (fe, fe.results()[0])
+        floods[prec] = fe.flood_results()[0]
     p64 = _np(runs["fp64"][0].peak_h[0])
     p32 = _np(runs["fp32"][0].peak_h[0])
     wet = (p64 > 1e-3) | (p32 > 1e-3)
@@ -157,6 +160,12 @@ def test_fp32_production_form_against_fp64():
           f"final volume rel. error {vol_err:.2e}; steps fp64 {r64.steps} fp32 {r32.steps}")
     assert rmse <= 0.01
     assert vol_err < 1e-3
+    m = compare(floods["fp32"], floods["fp64"])
+    print({k: v for k, v in m.items()})
+    assert m["arrival_cells"] > 0
+    assert m["arrival_rmse_s"] <= 60.0
+    assert m["arrival_cells_in_one_run_only"] <= 0.01 * m["arrival_cells"] + 1
+    assert m["peak_depth_rmse_m"] <= 0.01
 
 
 @pytest.mark.parametrize("dtype,tol", [(torch.float64, 1e-9), (torch.float32, 1e-5)])
