@@ -70,3 +70,17 @@ def test_chain_split_matches_the_engine_rule():
     shares = [sum(uneven[x:y]) for x, y in zip(b[:-1], b[1:])]
     assert max(shares) <= tot / 4 + 56
     assert chain_bounds([5, 1, 1], 3) == [0, 1, 2, 3]
+
+
+def test_default_chain_rule_of_the_library():
+    """his_engine_default_chains (called here without a GPU): one chain per 256
+    strip-chunk tiles, at least 1, at most 8 and at most one per member."""
+    from his_gb300 import _lib
+    lib = _lib.load()
+    rule = lib.his_engine_default_chains
+    assert rule(64, 3136) == 8            # 64 x 400x325 in 58 x 48 tiles
+    assert rule(64, 2368) == 8
+    assert rule(6, 300) == 1              # a small served batch
+    assert rule(2, 10000) == 2
+    assert rule(100, 1000) == 3
+    assert rule(1, 0) == 1
