@@ -174,6 +174,36 @@ EXCHANGE_CASES = {"exchange_overtop": dict(dx=100.0, seed=11, calls=6, dt=5.0)}
 COUPLED_CASES = {"coupled_overtop": dict(dx=100.0, steps=80, t_end=7200.0, snap_at=(1, 40, 80))}
 
 
+# Two members of the overtopping case batched in one reference CoupledEngine (one
+# shared dt, as the reference steps a batch): per-member roughness, channel
+# conveyance (apply_gamma), flooded-strip depth, initial channel level, inflow scale
+# and rain.
+COUPLED_BATCH_CASES = {"coupled_overtop_b2": dict(dx=100.0, steps=80, t_end=7200.0, snap_at=(1, 40, 80),
+                                                  gamma=(1.0, 1.44), manning=(0.04, 0.055),
+                                                  strip_depth=(0.4, 0.7), level_offset=(0.8, 1.1),
+                                                  inflow_scale=(1.0, 0.6), rain_mmh=(90.0, 50.0))}
+
+
+def rain_fn_batch(spec):
+    r = np.asarray(spec["rain_mmh"], dtype=np.float64) * MMH
+
+    def rain(t):
+        return r.copy() if 60.0 <= t < 600.0 else np.zeros_like(r)
+    return rain
+
+
+def inflow_batch(spec):
+    s = np.asarray(spec["inflow_scale"], dtype=np.float64)
+
+    def q(t):
+        return s * overtop_inflow(t)
+    return q
+
+
+def coupled_h0_batch(spec, z):
+    return np.stack([coupled_h0(spec, z) * (d / 0.4) for d in spec["strip_depth"]])
+
+
 def rain_fn_coupled(spec):
     def rain(t):
         return 90.0 * MMH if 60.0 <= t < 600.0 else 0.0

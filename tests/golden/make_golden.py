@@ -170,6 +170,51 @@ def make_coupled(name: str):
     print(name, "steps", spec["steps"], "final t", t, "mass err", float(out["mass_err"]))
 
 
+def make_coupled_batch(name: str):
+    """Two members of the overtopping case in one batched reference CoupledEngine,
+    stepped with the reference's own shared CFL choice."""
+    import torch
+    from hydrointel.benchmarks.suite import _overtopping_case
+    from hydrointel.domain.channels import apply_gamma
+    from hydrointel.solver.boundaries import all_edges
+    from hydrointel.solver.coupling import CoupledEngine
+    from hydrointel.solver.swe1d import SWE1D
+    from hydrointel.solver.swe2d import SWE2D
+    spec = GC.COUPLED_BATCH_CASES[name]
+    cpu = torch.device("cpu")
+    eng0, one0, two0 = _overtopping_case(cpu, dx=spec["dx"])
+    cfg = eng0.cfg
+    B = len(spec["gamma"])
+    z = _t(two0.z)
+    n_b = np.stack([np.full(z.shape, m) for m in spec["manning"]])
+    two = SWE2D(z, n_b, spec["dx"], cfg, all_edges("closed"), cpu, torch.float64, batch=B)
+    nets = [apply_gamma(one0.net, [g]) for g in spec["gamma"]]
+    one = SWE1D(nets, cfg, cpu, inflow=GC.inflow_batch(spec), stage=one0.stage)
+    off = torch.as_tensor(spec["level_offset"], dtype=torch.float64)[:, None]
+    one.set_level(one.z + off)
+    eng = CoupledEngine(two, one, cfg, rain=GC.rain_fn_batch(spec))
+    two.set_state(torch.as_tensor(GC.coupled_h0_batch(spec, z)))
+    eng.mb = type(eng.mb)(two.device, eng.total_volume())
+    rec = {k: [] for k in ("dt", "n_sub", "t")}
+    t = 0.0
+    out = {"h0": _t(two.h), "A0": _t(one.A), "Q0": _t(one.Q)}
+    for k in range(spec["steps"]):
+        dt = min(two.max_dt(), spec["t_end"] - t)
+        n_sub = max(1, math.ceil(dt / one.max_dt() - 1e-9))
+        rec["dt"].append(dt); rec["n_sub"].append(n_sub); rec["t"].append(t)
+        t = eng.step(t, spec["t_end"], dt=dt, n_sub=n_sub)
+        if k + 1 in spec["snap_at"]:
+            out[f"h_{k + 1}"], out[f"hu_{k + 1}"], out[f"hv_{k + 1}"] = _t(two.h), _t(two.hu), _t(two.hv)
+            out[f"A_{k + 1}"], out[f"Q_{k + 1}"] = _t(one.A), _t(one.Q)
+    src = eng.mb.sources()
+    for k, v in src.items():
+        out[f"src_{k}"] = np.asarray(v, dtype=np.float64)
+    out["mass_err"] = np.asarray(eng.mb.check(eng.total_volume(), t, record=False))
+    out.update({k: np.asarray(v) for k, v in rec.items()})
+    np.savez_compressed(HERE / f"{name}.npz", **out)
+    print(name, "steps", spec["steps"], "final t", t, "n_sub max", max(rec["n_sub"]), "mass err", out["mass_err"])
+
+
 def main(argv):
     ref = Path(argv[1] if len(argv) > 1 else "/root/reference")
     sys.path.insert(0, str(ref))
@@ -183,6 +228,8 @@ def main(argv):
         make_exchange(name)
     for name in GC.COUPLED_CASES:
         make_coupled(name)
+    for name in GC.COUPLED_BATCH_CASES:
+        make_coupled_batch(name)
 
 
 if __name__ == "__main__":

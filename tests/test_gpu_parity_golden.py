@@ -209,3 +209,43 @@ def test_coupled_step_sees_state_written_between_steps():
     dt, n_sub = expected(t)
     t = eng.step(t, spec["t_end"])
     assert eng._last_dt == dt and eng._last_n_sub == n_sub
+
+
+def test_batched_coupled_engine_matches_reference():
+    """The batched drop-in CoupledEngine (two members with their own roughness,
+    channel conveyance, states, inflow and rain; one shared CFL step) against the
+    reference's batched run: the same dt and substep sequence, chosen by the step
+    itself, and the same states and per-member mass terms."""
+    import his_gb300.channels as CH
+    from his_gb300.boundaries import all_edges
+    from his_gb300.coupling import CoupledEngine, build_links
+    from his_gb300.swe1d import SWE1D
+    from his_gb300.swe2d import SWE2D
+    fx_x = H.load("exchange_overtop")
+    fx = H.load("coupled_overtop_b2")
+    spec = GC.COUPLED_BATCH_CASES["coupled_overtop_b2"]
+    p = H.overtop_parts(fx_x)
+    B = len(spec["gamma"])
+    n_b = np.stack([np.full(p.z2d.shape, m) for m in spec["manning"]])
+    two = SWE2D(p.z2d, n_b, p.dx, p.cfg, all_edges("closed"), batch=B)
+    nets = [CH.apply_gamma(H.overtop_network(CH), [g]) for g in spec["gamma"]]
+    one = SWE1D(nets, p.cfg, inflow=GC.inflow_batch(spec), stage=p.stage)
+    links = build_links(one, two)
+    two.set_state(fx["h0"])
+    one.A = torch.as_tensor(fx["A0"])
+    one.Q = torch.as_tensor(fx["Q0"])
+    eng = CoupledEngine(two, one, p.cfg, rain=GC.rain_fn_batch(spec), links=links)
+    t = 0.0
+    for k in range(spec["steps"]):
+        t = eng.step(t, spec["t_end"])
+        assert eng._last_dt == pytest.approx(float(fx["dt"][k]), rel=1e-12), f"step {k}: dt"
+        assert eng._last_n_sub == int(fx["n_sub"][k]), f"step {k}: n_sub"
+        if k + 1 in spec["snap_at"]:
+            for f in ("h", "hu", "hv"):
+                assert H.max_abs(_np(getattr(two, f)), fx[f"{f}_{k + 1}"]) <= 1e-11, f"step {k + 1}: {f}"
+            assert H.max_abs(_np(one.A), fx[f"A_{k + 1}"]) <= 1e-10
+            assert H.max_abs(_np(one.Q), fx[f"Q_{k + 1}"]) <= 1e-10
+    src = eng.mb.sources()
+    for term in ("rain", "infiltration", "bnd2d_in", "bnd2d_out", "bnd1d_in", "bnd1d_out", "clip"):
+        want = np.asarray(fx[f"src_{term}"], dtype=np.float64)
+        assert np.allclose(np.asarray(src[term]), want, rtol=1e-10, atol=1e-9), term

@@ -114,3 +114,39 @@ def test_coupled_matches_reference():
 
 
 GC_TERMS = ("rain", "infiltration", "bnd2d_in", "bnd2d_out", "bnd1d_in", "bnd1d_out", "clip")
+
+
+def test_batched_coupled_members_match_reference():
+    """Each member of the reference's batched coupled run (shared dt; per-member
+    roughness, channel conveyance, states, inflow and rain), replayed by the oracle
+    member by member through the reference's dt and substep sequence."""
+    import his_gb300.channels as CH
+    from his_gb300.boundaries import all_edges
+    from his_gb300.topology import build_topology
+    from oracle.oracle import OracleCoupled, OracleLinks, OracleSWE1D, OracleSWE2D
+    fx_x = H.load("exchange_overtop")
+    fx = H.load("coupled_overtop_b2")
+    spec = GC.COUPLED_BATCH_CASES["coupled_overtop_b2"]
+    p = H.overtop_parts(fx_x)
+    rain, inflow = GC.rain_fn_batch(spec), GC.inflow_batch(spec)
+    for b, (gamma, manning) in enumerate(zip(spec["gamma"], spec["manning"])):
+        two = OracleSWE2D(p.z2d, np.full(p.z2d.shape, manning), p.dx, p.cfg, all_edges("closed"))
+        tp = build_topology(CH.apply_gamma(H.overtop_network(CH), [gamma]))
+        one = OracleSWE1D(tp, p.cfg, inflow=lambda t, b=b: float(inflow(t)[b]), stage=p.stage)
+        links = OracleLinks(**p.links)
+        two.set_state(fx["h0"][b])
+        one.A = np.ascontiguousarray(fx["A0"][b].reshape(one.A.shape))
+        one.Q = np.ascontiguousarray(fx["Q0"][b].reshape(one.Q.shape))
+        eng = OracleCoupled(two, one, links, p.cfg, rain=lambda t, b=b: float(rain(t)[b]))
+        t = 0.0
+        for k in range(spec["steps"]):
+            t = eng.step(t, spec["t_end"], dt=float(fx["dt"][k]), n_sub=int(fx["n_sub"][k]))
+            if k + 1 in spec["snap_at"]:
+                for f in ("h", "hu", "hv"):
+                    want = fx[f"{f}_{k + 1}"][b]
+                    assert H.max_abs(getattr(two, f).reshape(want.shape), want) <= 1e-11, (b, k + 1, f)
+                assert H.max_abs(one.A.reshape(-1), fx[f"A_{k + 1}"][b]) <= 1e-10, (b, k + 1)
+                assert H.max_abs(one.Q.reshape(-1), fx[f"Q_{k + 1}"][b]) <= 1e-10, (b, k + 1)
+        for term in GC_TERMS:
+            want = float(fx[f"src_{term}"][b])
+            assert float(eng.acc[term][0]) == pytest.approx(want, rel=1e-10, abs=1e-9), (b, term)
