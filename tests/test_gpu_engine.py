@@ -219,3 +219,40 @@ def test_member_chains_do_not_change_results():
         for a, b in zip(states[1][0], states[chains][0]):
             assert np.array_equal(a, b), f"{chains} chains: state differs"
         assert states[1][1] == states[chains][1] and states[1][2] == states[chains][2]
+
+
+@pytest.mark.parametrize("order", [1, 2])
+def test_grid_step_parts_match_members_alone(order):
+    """A drop-in grid step large enough to run its stage launches as parts (48 members
+    of 100 x 81 cells in 58 x 16 tiles: 576 tiles, 2 parts) equals each member
+    stepped alone, bit for bit, at first order (stage copy per part) and second."""
+    from his_gb300 import workloads as W
+    from his_gb300.boundaries import all_edges
+    from his_gb300.config import SolverConfig
+    from his_gb300.swe2d import SWE2D
+    ter = W.plain_small().terrain
+    z = ter.z
+    B = 48
+    cfg = SolverConfig(spatial_order=order)
+    rng = np.random.default_rng(5)
+    n = rng.uniform(0.02, 0.06, B)[:, None, None] * np.ones((B,) + z.shape)
+    eta = float(np.quantile(z, 0.3)) + rng.uniform(0.0, 2.0, B)
+    h0 = np.maximum(eta[:, None, None] - z[None], 0.0)
+    bcs = all_edges("transmissive")
+    batched = SWE2D(z, n, ter.dx, cfg, bcs, batch=B, tile=(58, 16))
+    batched.set_state(h0)
+    dts, vols = [], []
+    for k in range(12):
+        dt = batched.max_dt()
+        dts.append(dt)
+        v = batched.step(dt, 60.0 * k, 2e-5)
+        vols.append(np.stack([_np(getattr(v, f)) for f in ("bnd_in", "bnd_out", "rain", "infil", "clip")]))
+    for b in range(0, B, 7):
+        one = SWE2D(z, n[b], ter.dx, cfg, bcs, tile=(58, 16))
+        one.set_state(h0[b])
+        for k, dt in enumerate(dts):
+            v = one.step(dt, 60.0 * k, 2e-5)
+            got = np.array([float(getattr(v, f)) for f in ("bnd_in", "bnd_out", "rain", "infil", "clip")])
+            assert np.array_equal(got, vols[k][:, b]), f"member {b}, step {k}: volumes"
+        for f in ("h", "hu", "hv"):
+            assert np.array_equal(_np(getattr(one, f)), _np(getattr(batched, f)[b])), f"member {b}: {f}"
