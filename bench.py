@@ -114,29 +114,90 @@ def peaks():
 
 
 class ClockSampler:
-    """nvidia-smi clocks and throttle reasons every 200 ms while the timed region runs."""
+    """SM clocks and throttle reasons sampled during the timed region.
 
+    NVML (the driver's libnvidia-ml, read-only queries) is polled every millisecond
+    from a host thread, so even a timed region of a few milliseconds gets several
+    samples; without NVML, nvidia-smi every 200 ms."""
+
+    REASONS = {0x4: "sw_power_cap", 0x8: "hw_slowdown", 0x20: "sw_thermal_slowdown", 0x40: "hw_thermal_slowdown"}
     FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
               "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
               "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
 
-    def __init__(self, gpu_index: int):
+    def __init__(self, gpu_index: int, period_s: float = 0.001):
         self.gpu = gpu_index
+        self.period = period_s
+        self.samples = []            # (sm_mhz, reason bits)
+        self.max_mhz = None
+        self.source = None
+        self._nvml = None
+        self._stop = None
+        self._thread = None
         self.proc = None
         self.path = None
 
+    def _nvml_open(self):
+        import ctypes as C
+        try:
+            lib = C.CDLL("libnvidia-ml.so.1")
+        except OSError:
+            return None
+        if lib.nvmlInit_v2() != 0:
+            return None
+        h = C.c_void_p()
+        if lib.nvmlDeviceGetHandleByIndex_v2(C.c_uint(self._nvml_index()), C.byref(h)) != 0:
+            return None
+        mx = C.c_uint()
+        if lib.nvmlDeviceGetMaxClockInfo(h, C.c_int(1), C.byref(mx)) == 0:
+            self.max_mhz = float(mx.value)
+        reasons = getattr(lib, "nvmlDeviceGetCurrentClocksEventReasons", None) or \
+            getattr(lib, "nvmlDeviceGetCurrentClocksThrottleReasons")
+        return lib, h, reasons
+
+    def _nvml_index(self) -> int:
+        vis = os.environ.get("CUDA_VISIBLE_DEVICES", "")
+        ids = [v.strip() for v in vis.split(",") if v.strip()]
+        if ids and all(v.isdigit() for v in ids) and self.gpu < len(ids):
+            return int(ids[self.gpu])
+        return self.gpu
+
+    def _poll(self):
+        import ctypes as C
+        lib, h, reasons = self._nvml
+        mhz, bits = C.c_uint(), C.c_ulonglong()
+        while not self._stop.is_set():
+            if lib.nvmlDeviceGetClockInfo(h, C.c_int(1), C.byref(mhz)) == 0 and reasons(h, C.byref(bits)) == 0:
+                self.samples.append((float(mhz.value), int(bits.value)))
+            self._stop.wait(self.period)
+
     def __enter__(self):
+        import threading
+        try:
+            self._nvml = self._nvml_open()
+        except Exception:
+            self._nvml = None
+        if self._nvml is not None:
+            self.source = "nvml, 1 ms"
+            self._stop = threading.Event()
+            self._thread = threading.Thread(target=self._poll, daemon=True)
+            self._thread.start()
+            return self
         fd, self.path = tempfile.mkstemp(suffix=".csv")
         os.close(fd)
         try:
             self.proc = subprocess.Popen(["nvidia-smi", f"--id={self.gpu}", f"--query-gpu={self.FIELDS}",
                                           "--format=csv,noheader,nounits", "-lms", "200"],
                                          stdout=open(self.path, "w"), stderr=subprocess.DEVNULL)
+            self.source = "nvidia-smi, 200 ms"
         except Exception:
             self.proc = None
         return self
 
     def __exit__(self, *exc):
+        if self._thread is not None:
+            self._stop.set()
+            self._thread.join(timeout=5)
         if self.proc is not None:
             self.proc.terminate()
             try:
@@ -145,6 +206,13 @@ class ClockSampler:
                 self.proc.kill()
 
     def summary(self):
+        if self._nvml is not None:
+            if not self.samples:
+                return None
+            sm = [m for m, _ in self.samples]
+            reasons = sorted({n for _, b in self.samples for bit, n in self.REASONS.items() if b & bit})
+            return {"sm_mhz": statistics.median(sm), "sm_max_mhz": self.max_mhz or max(sm), "samples": len(sm),
+                    "reasons": reasons, "source": self.source}
         if not self.path or not Path(self.path).exists():
             return None
         rows = [r.split(",") for r in Path(self.path).read_text().strip().splitlines() if r.strip()]
@@ -166,12 +234,16 @@ class ClockSampler:
         if not sm:
             return None
         return {"sm_mhz": statistics.median(sm), "sm_max_mhz": max(mx), "samples": len(sm),
-                "reasons": sorted(reasons)}
+                "reasons": sorted(reasons), "source": self.source}
+
+
+TRAFFIC_PROFILE = "profiles/strip_kernel_f32_batched_uniform.md"
 
 
 def read_traffic():
-    """Per-cell DRAM traffic of the dominant kernel from the committed ncu summary."""
-    p = ROOT / "profiles" / "strip_kernel_f32_batched_uniform.md"
+    """Per-cell DRAM traffic of the dominant kernel, as measured by the ncu capture that
+    the committed summary records (not by this run: counters are not read live)."""
+    p = ROOT / TRAFFIC_PROFILE
     if not p.exists():
         return None
     for line in p.read_text().splitlines():
@@ -281,6 +353,29 @@ def accuracy_leg(interval_s: float = 60.0) -> dict:
     return m
 
 
+def accuracy_c3_leg(members: int = 2, interval_s: float = 120.0) -> dict:
+    """Error of the float32 production form against the float64 method at full
+    resolution: the first ``members`` storms of the 64-storm batch (400 x 325 @ 20 m)
+    run to their end in both precisions (his_gb300.accuracy.against_fp64): peak depth
+    (max and RMSE over wet cells), arrival time at 0.1 m from the outputs, volume and
+    both runs' mass-balance errors."""
+    from his_gb300 import workloads as W
+    from his_gb300.accuracy import against_fp64
+    w0 = time.perf_counter()
+    rows = against_fp64(W.batched_uniform(members), interval_s)
+    keep = ("member", "status_fp32", "status_fp64", "steps_fp32", "steps_fp64", "peak_depth_rmse_m",
+            "peak_depth_max_m", "peak_every_step_rmse_m", "wet_cells", "arrival_rmse_s", "arrival_max_s",
+            "arrival_cells", "arrival_cells_in_one_run_only", "final_volume_rel", "final_surface_volume_rel",
+            "mass_error_fp32", "mass_error_fp64")
+    return {"workload": f"{members} members of the 64-storm batch, 400x325 @ 20 m, 8.5 h storms to their end, "
+                        f"float32 production form against float64, outputs every {interval_s:.0f} s",
+            "peak_depth_rmse_m_max": max(r["peak_depth_rmse_m"] for r in rows),
+            "arrival_rmse_s_max": max(r["arrival_rmse_s"] for r in rows),
+            "mass_error_fp32_max": max(r["mass_error_fp32"] for r in rows),
+            "members": [{k: r[k] for k in keep if k in r} for r in rows],
+            "wall_s": time.perf_counter() - w0}
+
+
 def e2e_dropin(storms, steps: int):
     """Same metric through the drop-in public API (batched CoupledEngine -> C ABI, host
     buffers): every step uploads its step parameters and 1-D forcing from host memory
@@ -329,7 +424,11 @@ def run_ours(args, world, rank, local):
     cells = sum(s.cells for s in storms)
     tile = "auto" if args.tile == "auto" else tuple(int(v) for v in args.tile.split("x"))
     eng = FloodEngine(storms, SolverConfig(), precision="fp32", graph_steps=16, tile=tile, chains=args.chains)
+    # graphs are captured before the steps they run: the warm-up's, then the timed
+    # region's (a whole number of 16-step graphs plus one remainder graph per chain)
+    eng.prepare(args.warmup)
     eng.advance(args.warmup)
+    eng.prepare(args.steps)
     torch.cuda.synchronize()
     s = torch.cuda.current_stream()
     ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
@@ -367,6 +466,8 @@ def run_ours(args, world, rank, local):
            "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s",
                         "frac": achieved / hbm, "peak_kind": peak_kind,
                         "traffic": traffic * cells if traffic is not None else None,
+                        "traffic_source": f"ncu capture of this kernel on this workload ({TRAFFIC_PROFILE}), "
+                                          "not this run",
                         "kernel": "strip_kernel<float,64,2> (RK stage 2 + sources + friction + CFL)",
                         "alg_bytes_per_cell": ALG_BYTES_F32,
                         "step_achieved": ALG_BYTES_F32 * cells / step_s / 1e9,
@@ -399,6 +500,8 @@ def run_ours(args, world, rank, local):
         out["uneven_batch"] = uneven_leg(args.storm_seconds)
         torch.cuda.empty_cache()
         out["accuracy_c1"] = accuracy_leg()
+        torch.cuda.empty_cache()
+        out["accuracy_c3"] = accuracy_c3_leg()
         torch.cuda.empty_cache()
         if args.serve_seconds > 0:
             out["serving"] = serving_leg(args.serve_seconds)
@@ -440,7 +543,9 @@ def run_reference(args, world, rank):
     return {"impl": "reference", "metric": "cell-steps/s", "value": value, "unit": "cell-steps/s", "n_gpus": world,
             "steps": steps, "warmup": args.warmup, "ms_per_step": wall * 1e3 / steps, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded terrain, forcing "
-            "and networks)", "config": workload_config(args.members),
+            "and networks)", "config": workload_config(args.members) | {
+                "sampled": "member 0 of the batch, one member-step per step (the rate is per member-cell-step)",
+                "precision": "fp64 throughout (the reference's method on the host)"},
             "cpu_baseline": {"value": value, "unit": "cell-steps/s", "cores": threads, "kind": "port",
                              "sample": f"{steps} coupled float64 steps of member 0 of the batch (400x325), "
                                        "the oracle restatement of the reference's step on all host threads"},

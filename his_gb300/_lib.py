@@ -17,6 +17,7 @@ from . import build as _build
 HIS_OK, HIS_ERR_BAD_ARG, HIS_ERR_NONFINITE, HIS_ERR_IMPLAUSIBLE = 0, 1, 2, 3
 HIS_ERR_WAIT_TIMEOUT, HIS_ERR_OOM_ADMISSION, HIS_ERR_CUDA, HIS_ERR_UNSUPPORTED = 4, 5, 6, 7
 PREC_F64, PREC_F32 = 0, 1
+NOALLOC_SCRATCH_BYTES = 16 * 1024 * 1024     # HIS_NOALLOC_SCRATCH_BYTES
 
 _I32P = C.POINTER(C.c_int32)
 _I64P = C.POINTER(C.c_int64)
@@ -107,6 +108,7 @@ SIGNATURES = {
                                       C.POINTER(_H)]),
     "his_engine_destroy": (C.c_int32, [_H]),
     "his_engine_advance": (C.c_int32, [_H, C.c_int32, C.c_void_p]),
+    "his_engine_prepare": (C.c_int32, [_H, C.c_int32]),
     "his_engine_set_chains": (C.c_int32, [_H, C.c_int32]),
     "his_engine_chains": (C.c_int32, [_H]),
     "his_engine_default_chains": (C.c_int32, [C.c_int32, C.c_int32]),
@@ -132,6 +134,11 @@ def load():
                 fn.argtypes = args
             _LIB = L
     return _LIB
+
+
+def last_error() -> str:
+    """The library's message for the last failed call on this thread."""
+    return (load().his_last_error() or b"").decode(errors="replace")
 
 
 def check(rc: int, what: str) -> None:

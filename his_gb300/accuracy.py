@@ -72,4 +72,41 @@ def compare(test, ref, threshold: float = 0.1, wet: float = 1e-3) -> dict:
     }
 
 
-__all__ = ["arrival_times", "compare"]
+def against_fp64(storms, interval_s: float, cfg=None, chunk: int = 1024, timeout_s: float | None = None):
+    """Run ``storms`` to their end twice through the device engine, in the float32
+    production form and in the float64 method, with outputs every ``interval_s``, and
+    compare each member (``compare``).  Each member keeps its own dt, so a member's
+    arithmetic does not depend on the batch it runs in.  Returns one dict per member
+    with the comparison, both runs' mass-balance errors, statuses and step counts."""
+    from .config import SolverConfig
+    from .engine import FloodEngine
+    runs = {}
+    for prec in ("fp64", "fp32"):
+        c = cfg or SolverConfig(slot_width_frac=storms[0].slot_width_frac)
+        fe = FloodEngine(list(storms), c, precision=prec, track_peaks=True, output_interval=interval_s)
+        reps = fe.run(chunk=chunk, timeout_s=timeout_s)
+        res = fe.results(reps)
+        runs[prec] = (fe.flood_results(reps), res)
+        fe.close()
+    out = []
+    for b, s in enumerate(storms):
+        (f64, r64), (f32, r32) = (runs["fp64"][0][b], runs["fp64"][1][b]), (runs["fp32"][0][b], runs["fp32"][1][b])
+        m = compare(f32, f64)
+        # the running maxima over every step, beside the maxima over the output times
+        e32, e64 = f32.extras.get("depth_max_every_step"), f64.extras.get("depth_max_every_step")
+        if e32 is not None and e64 is not None:
+            a, b_ = _np(e32), _np(e64)
+            wet = (a > 1e-3) | (b_ > 1e-3)
+            d = (a - b_)[wet]
+            m["peak_every_step_rmse_m"] = float(np.sqrt(np.mean(d ** 2))) if d.size else 0.0
+            m["peak_every_step_max_m"] = float(np.abs(d).max()) if d.size else 0.0
+        m.update({"member": s.key, "grid": f"{s.terrain.nx}x{s.terrain.ny}", "t_end_s": float(s.t_end),
+                  "status_fp32": r32.status, "status_fp64": r64.status, "steps_fp32": r32.steps,
+                  "steps_fp64": r64.steps, "mass_error_fp32": float(r32.mass_error),
+                  "mass_error_fp64": float(r64.mass_error),
+                  "final_volume_rel": abs(r32.volume - r64.volume) / max(abs(r64.volume), 1.0)})
+        out.append(m)
+    return out
+
+
+__all__ = ["arrival_times", "compare", "against_fp64"]

@@ -238,7 +238,18 @@ static int grid_parts_setup(his_grid* g) {
         e = cudaStreamCreateWithFlags(&g->ps[k], cudaStreamNonBlocking);
         if (e == cudaSuccess) e = cudaEventCreateWithFlags(&g->pev_join[k], cudaEventDisableTiming);
     }
-    if (e != cudaSuccess) return cuda_fail(e, "grid step: part streams");
+    if (e != cudaSuccess) {
+        // release what was made, so that a later step retries from a clean slate
+        for (int k = 0; k + 1 < his_grid::MAX_PARTS; ++k) {
+            if (g->ps[k]) cudaStreamDestroy(g->ps[k]);
+            if (g->pev_join[k]) cudaEventDestroy(g->pev_join[k]);
+            g->ps[k] = nullptr;
+            g->pev_join[k] = nullptr;
+        }
+        if (g->pev_fork) cudaEventDestroy(g->pev_fork);
+        g->pev_fork = nullptr;
+        return cuda_fail(e, "grid step: part streams");
+    }
     g->part_t[0] = 0;
     int m = 0;
     for (int k = 1; k < np; ++k) {
@@ -259,10 +270,7 @@ static int fill_params(his_grid* g, const his_step_params* p, StepParams* sp) {
         sp[m].snap_k = -1;
         if (!std::isfinite(q.dt) || !(q.dt >= 0) || !std::isfinite(q.t) || !std::isfinite(q.rain))
             return bad("member " + std::to_string(m) + ": dt, t and rain must be finite (dt >= 0)");
-        sp[m].dt = q.dt; sp[m].t = q.t; sp[m].rain = q.rain;
-        for (int e = 0; e < 4; ++e) { sp[m].bc0[e] = q.bc_t[e]; sp[m].bc1[e] = q.bc_t_dt[e]; }
-        sp[m].active = 1;
-        params_set_f32(sp[m]);
+        sp[m] = step_params_from(q);
     }
     return HIS_OK;
 }
@@ -707,7 +715,10 @@ static int engine_split(his_engine* E, int n) {
         cudaGraphExec_t& x = E->exec_of(c);
         if (x) cudaGraphExecDestroy(x);
         x = nullptr;
+        if (E->rexec[c]) cudaGraphExecDestroy(E->rexec[c]);
+        E->rexec[c] = nullptr;
     }
+    E->rem_steps = 0;
     E->n_chains = n;
     E->chain_m[0] = 0;
     E->chain_t[0] = 0;
@@ -736,6 +747,8 @@ int32_t his_engine_destroy(his_engine* E) {
     }
     if (E->exec) cudaGraphExecDestroy(E->exec);
     for (cudaGraphExec_t x : E->cexec)
+        if (x) cudaGraphExecDestroy(x);
+    for (cudaGraphExec_t x : E->rexec)
         if (x) cudaGraphExecDestroy(x);
     cudaFree(E->d_em);
     cudaFree(E->d_arena);
@@ -860,12 +873,12 @@ static int engine_enqueue(his_engine* E, int chain, int n) {
     return E->grid->prec == HIS_PREC_F64 ? engine_enqueue_f64(E, chain, n) : engine_enqueue_f32(E, chain, n);
 }
 
-// One graph of graph_steps steps of one chain, captured from the chain's main stream.
-static int engine_capture(his_engine* E, int chain, cudaGraphExec_t* exec) {
+// One graph of n_steps steps of one chain, captured from the chain's main stream.
+static int engine_capture(his_engine* E, int chain, int n_steps, cudaGraphExec_t* exec) {
     cudaStream_t s = E->main_of(chain);
     cudaGraph_t graph = nullptr;
     HIS_CK(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
-    int rc = engine_enqueue(E, chain, E->graph_steps);
+    int rc = engine_enqueue(E, chain, n_steps);
     cudaError_t ce = cudaStreamEndCapture(s, &graph);
     if (rc) { if (graph) cudaGraphDestroy(graph); return rc; }
     if (ce != cudaSuccess) return cuda_fail(ce, "his_engine_advance: capture");
@@ -875,32 +888,52 @@ static int engine_capture(his_engine* E, int chain, cudaGraphExec_t* exec) {
     return HIS_OK;
 }
 
+// Make sure the graphs an advance of n_steps launches exist: the graph_steps graph of
+// every chain (when n_steps reaches it) and the graphs of the remaining
+// n_steps % graph_steps steps (one remainder size is kept; another size replaces it).
+static int engine_graphs(his_engine* E, int n_steps) {
+    const int nc = E->n_chains;
+    if (n_steps >= E->graph_steps && !E->exec) {
+        for (int c = 0; c < nc; ++c) {
+            int rc = engine_capture(E, c, E->graph_steps, &E->exec_of(c));
+            if (rc) return rc;
+        }
+    }
+    const int rem = n_steps % E->graph_steps;
+    if (rem && rem != E->rem_steps) {
+        E->rem_steps = 0;
+        for (int c = 0; c < nc; ++c) {
+            if (E->rexec[c]) cudaGraphExecDestroy(E->rexec[c]);
+            E->rexec[c] = nullptr;
+            int rc = engine_capture(E, c, rem, &E->rexec[c]);
+            if (rc) return rc;
+        }
+        E->rem_steps = rem;
+    }
+    return HIS_OK;
+}
+
+int32_t his_engine_prepare(his_engine* E, int32_t n_steps) {
+    if (!E) return bad("engine is NULL");
+    if (n_steps < 0) return bad("n_steps must be >= 0");
+    return engine_graphs(E, n_steps);
+}
+
 int32_t his_engine_advance(his_engine* E, int32_t n_steps, void* stream) {
     if (!E) return bad("engine is NULL");
     if (n_steps < 0) return bad("n_steps must be >= 0");
     cudaStream_t caller = (cudaStream_t)stream;
     const int nc = E->n_chains;
+    int rc = engine_graphs(E, n_steps);
+    if (rc) return rc;
     HIS_CK(cudaEventRecord(E->ev_in, caller));
     for (int c = 0; c < nc; ++c) HIS_CK(cudaStreamWaitEvent(E->main_of(c), E->ev_in, 0));
-    if (!E->exec && n_steps >= E->graph_steps) {
-        for (int c = 0; c < nc; ++c) {
-            int rc = engine_capture(E, c, &E->exec_of(c));
-            if (rc) return rc;
-        }
-    }
     // the chains run independently until the end of the call, each launching its
     // graphs back to back on its own stream, so their relative phase is kept
-    int done = 0;
-    if (E->exec) {
-        for (; done + E->graph_steps <= n_steps; done += E->graph_steps)
-            for (int c = 0; c < nc; ++c) HIS_CK(cudaGraphLaunch(E->exec_of(c), E->main_of(c)));
-    }
-    if (done < n_steps) {
-        for (int c = 0; c < nc; ++c) {
-            int rc = engine_enqueue(E, c, n_steps - done);
-            if (rc) return rc;
-        }
-    }
+    for (int done = 0; done + E->graph_steps <= n_steps; done += E->graph_steps)
+        for (int c = 0; c < nc; ++c) HIS_CK(cudaGraphLaunch(E->exec_of(c), E->main_of(c)));
+    if (n_steps % E->graph_steps)
+        for (int c = 0; c < nc; ++c) HIS_CK(cudaGraphLaunch(E->rexec[c], E->main_of(c)));
     for (int c = 0; c < nc; ++c) {
         HIS_CK(cudaEventRecord(E->out_of(c), E->main_of(c)));
         HIS_CK(cudaStreamWaitEvent(caller, E->out_of(c), 0));

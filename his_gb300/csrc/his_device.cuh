@@ -136,6 +136,24 @@ __host__ __device__ inline void params_set_f32(StepParams& p) {
     }
 }
 
+// The step record of one member from the ABI's step parameters: every field set
+// (snapshot slot -1 and no snapshot pointers: no output at the end of this step), the
+// float32 copies formed here.  Every producer of records on the host uses it.
+inline StepParams step_params_from(const his_step_params& q) {
+    StepParams sp{};
+    sp.snap_k = -1;
+    sp.dt = q.dt;
+    sp.t = q.t;
+    sp.rain = q.rain;
+    for (int e = 0; e < 4; ++e) {
+        sp.bc0[e] = q.bc_t[e];
+        sp.bc1[e] = q.bc_t_dt[e];
+    }
+    sp.active = 1;
+    params_set_f32(sp);
+    return sp;
+}
+
 struct TileRef {
     int member, x0, y0, local;
 };

@@ -101,6 +101,10 @@ struct his_engine {
     cudaStream_t cs_main[MAX_CHAINS - 1] = {}, cs_side[MAX_CHAINS - 1] = {};
     cudaEvent_t cev_fork[MAX_CHAINS - 1] = {}, cev_join[MAX_CHAINS - 1] = {}, cev_out[MAX_CHAINS - 1] = {};
     cudaGraphExec_t cexec[MAX_CHAINS - 1] = {};
+    // graphs of rem_steps < graph_steps steps, one per chain, for advances whose step
+    // count is not a multiple of graph_steps (0: none captured)
+    int rem_steps = 0;
+    cudaGraphExec_t rexec[MAX_CHAINS] = {};
     cudaStream_t main_of(int c) const { return c == 0 ? s0 : cs_main[c - 1]; }
     cudaStream_t side_of(int c) const { return c == 0 ? s1 : cs_side[c - 1]; }
     cudaEvent_t fork_of(int c) const { return c == 0 ? ev_fork : cev_fork[c - 1]; }

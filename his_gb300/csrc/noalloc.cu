@@ -8,10 +8,14 @@
 // step needs come from one array of HIS_NOALLOC_SCRATCH_BYTES bytes compiled into
 // this library, which every GPU the library runs on holds for the life of the process.
 //
-// The first call on each device, with that device current, looks up the array's
-// device address with cudaGetSymbolAddress and keeps it; that first call is the
-// set-up and should come before any stream capture.  Grids whose scratch would not fit
-// the array are rejected with HIS_ERR_BAD_ARG before any work is queued.
+// The array's device address belongs to one CUDA context.  The first call in each
+// context (the device's primary context, or a context the host application made
+// itself and made current) looks the address up with cudaGetSymbolAddress and keeps
+// it under the context's unique ID, so a later context -- after cudaDeviceReset, or a
+// second context the application creates -- gets its own lookup and never an address
+// of another context.  That first call per context is the set-up and should come
+// before any stream capture.  Grids whose scratch would not fit the array are rejected
+// with HIS_ERR_BAD_ARG before any work is queued.
 //
 // Every call clears the partial sums and totals it reads, so nothing in the array has
 // to start at zero; the state arrays (h, hu, hv, s_filled, infil_cum) and the optional
@@ -20,8 +24,11 @@
 // without an event between them, or from two host threads) race on it and give wrong
 // results.  Order them on one stream.
 #include <cmath>
+#include <cstdint>
 #include <mutex>
 #include <string>
+
+#include <cuda.h>
 
 #include "his_internal.h"
 #include "swe2d_strip.cuh"
@@ -30,31 +37,74 @@ namespace his {
 
 static __device__ __align__(256) unsigned char g_noalloc_scratch[HIS_NOALLOC_SCRATCH_BYTES];
 
-constexpr int kNoallocMaxDevices = 64;
-static unsigned char* g_noalloc_base[kNoallocMaxDevices] = {};
+// Current context and its process-unique ID, through the driver entry points that
+// the runtime hands out (the library links the runtime only).
+using CtxGetCurrentFn = CUresult (*)(CUcontext*);
+using CtxGetIdFn = CUresult (*)(CUcontext, unsigned long long*);
+static CtxGetCurrentFn g_ctx_current = nullptr;
+static CtxGetIdFn g_ctx_id = nullptr;
+static std::once_flag g_ctx_once;
+
+static void load_ctx_entry_points() {
+    void* f = nullptr;
+    cudaDriverEntryPointQueryResult q{};
+    if (cudaGetDriverEntryPointByVersion("cuCtxGetCurrent", &f, 12000, cudaEnableDefault, &q) == cudaSuccess &&
+        q == cudaDriverEntryPointSuccess)
+        g_ctx_current = reinterpret_cast<CtxGetCurrentFn>(f);
+    f = nullptr;
+    if (cudaGetDriverEntryPointByVersion("cuCtxGetId", &f, 12000, cudaEnableDefault, &q) == cudaSuccess &&
+        q == cudaDriverEntryPointSuccess)
+        g_ctx_id = reinterpret_cast<CtxGetIdFn>(f);
+    cudaGetLastError();
+}
+
+// Key of the current context (0: none current yet, or the lookup is unavailable).
+static unsigned long long current_ctx_key() {
+    std::call_once(g_ctx_once, load_ctx_entry_points);
+    if (!g_ctx_current) return 0;
+    CUcontext ctx = nullptr;
+    if (g_ctx_current(&ctx) != CUDA_SUCCESS || !ctx) return 0;
+    unsigned long long id = 0;
+    if (g_ctx_id && g_ctx_id(ctx, &id) == CUDA_SUCCESS) return id + 1;
+    return (unsigned long long)(uintptr_t)ctx;
+}
+
+constexpr int kNoallocCache = 64;
+struct NoallocEntry {
+    unsigned long long ctx;
+    unsigned char* base;
+};
+static NoallocEntry g_noalloc_cache[kNoallocCache] = {};
+static int g_noalloc_next = 0;
 static std::mutex g_noalloc_mu;
 
-// Device address of the scratch array on the current device, looked up once per device.
+// Device address of the scratch array in the current context, looked up once per
+// context.  With no context current yet, the lookup itself brings up the device's
+// primary context (as any runtime call does), and the address is kept under that
+// context's key.  Without a context key (no driver entry points), the address is
+// looked up on every call.
 static int noalloc_base(unsigned char** out) {
-    int dev = -1;
-    HIS_CK(cudaGetDevice(&dev));
-    if (dev < 0 || dev >= kNoallocMaxDevices) {
-        set_error("his_grid_step_noalloc: device ordinal " + std::to_string(dev) + " beyond the " +
-                  std::to_string(kNoallocMaxDevices) + " devices it supports");
-        return HIS_ERR_UNSUPPORTED;
-    }
     std::lock_guard<std::mutex> lock(g_noalloc_mu);
-    if (!g_noalloc_base[dev]) {
-        void* p = nullptr;
-        cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
-        if (e != cudaSuccess) return cuda_fail(e, "his_grid_step_noalloc: cudaGetSymbolAddress");
-        if (!p) {
-            set_error("his_grid_step_noalloc: cudaGetSymbolAddress returned a null address");
-            return HIS_ERR_CUDA;
-        }
-        g_noalloc_base[dev] = static_cast<unsigned char*>(p);
+    unsigned long long key = current_ctx_key();
+    if (key)
+        for (const NoallocEntry& e : g_noalloc_cache)
+            if (e.ctx == key) {
+                *out = e.base;
+                return HIS_OK;
+            }
+    void* p = nullptr;
+    cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
+    if (e != cudaSuccess) return cuda_fail(e, "his_grid_step_noalloc: cudaGetSymbolAddress");
+    if (!p) {
+        set_error("his_grid_step_noalloc: cudaGetSymbolAddress returned a null address");
+        return HIS_ERR_CUDA;
     }
-    *out = g_noalloc_base[dev];
+    if (!key) key = current_ctx_key();
+    if (key) {
+        g_noalloc_cache[g_noalloc_next] = NoallocEntry{key, static_cast<unsigned char*>(p)};
+        g_noalloc_next = (g_noalloc_next + 1) % kNoallocCache;
+    }
+    *out = static_cast<unsigned char*>(p);
     return HIS_OK;
 }
 
@@ -109,11 +159,6 @@ extern "C" int32_t his_grid_step_noalloc(int32_t precision, const his_solver_cfg
     }
     const int nh = (d.f0 != nullptr) + (d.fc != nullptr) + (d.k != nullptr);
     if (nh != 0 && nh != 3) { set_error("f0, fc and k must be given together"); return HIS_ERR_BAD_ARG; }
-    const his_step_params& q = *params;
-    if (!std::isfinite(q.dt) || !(q.dt >= 0) || !std::isfinite(q.t) || !std::isfinite(q.rain)) {
-        set_error("dt, t and rain must be finite (dt >= 0)");
-        return HIS_ERR_BAD_ARG;
-    }
     const size_t elem = precision == HIS_PREC_F64 ? sizeof(double) : sizeof(float);
     if ((int64_t)d.ny * d.nx > ((int64_t)HIS_NOALLOC_SCRATCH_BYTES) / (3 * (int64_t)elem)) {
         set_error("his_grid_step_noalloc: a " + std::to_string(d.ny) + " x " + std::to_string(d.nx) +
@@ -127,6 +172,11 @@ extern "C" int32_t his_grid_step_noalloc(int32_t precision, const his_solver_cfg
                   " grid needs " + std::to_string(L.total) + " bytes of scratch, more than the " +
                   std::to_string((long long)HIS_NOALLOC_SCRATCH_BYTES) +
                   " it has; use his_grid_create for larger grids");
+        return HIS_ERR_BAD_ARG;
+    }
+    const his_step_params& q = *params;
+    if (!std::isfinite(q.dt) || !(q.dt >= 0) || !std::isfinite(q.t) || !std::isfinite(q.rain)) {
+        set_error("dt, t and rain must be finite (dt >= 0)");
         return HIS_ERR_BAD_ARG;
     }
     unsigned char* base = nullptr;

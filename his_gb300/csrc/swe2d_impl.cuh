@@ -371,16 +371,7 @@ int noalloc_step_impl(const Consts& c, const his_grid_desc& d, const his_step_pa
     G.z = (const R*)d.z; G.n = (const R*)d.manning; G.S = (const R*)d.storage;
     G.f0 = (const R*)d.f0; G.fc = (const R*)d.fc; G.k = (const R*)d.k; G.rw = (const R*)d.rain_weight;
     G.pk = (R*)d.peak_h; G.ps = (R*)d.peak_speed;
-    StepParams P{};
-    P.dt = p.dt;
-    P.t = p.t;
-    P.rain = p.rain;
-    for (int e = 0; e < 4; ++e) {
-        P.bc0[e] = p.bc_t[e];
-        P.bc1[e] = p.bc_t_dt[e];
-    }
-    P.active = 1;
-    params_set_f32(P);
+    const StepParams P = step_params_from(p);
     const int work = std::max(L.n_strips * (int)NPART, 8);
     noalloc_setup_kernel<R><<<(work + 255) / 256, 256, 0, s>>>(G, P, L, base);
     auto* grid = reinterpret_cast<const Grid<R>*>(base + L.o_grid);

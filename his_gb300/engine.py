@@ -420,6 +420,12 @@ class FloodEngine:
             _lib.check(self._lib.his_engine_advance(self._engine, int(n_steps), _lib.stream_handle()),
                        "his_engine_advance")
 
+    def prepare(self, n_steps: int) -> None:
+        """Capture the CUDA graphs that ``advance(n_steps)`` launches, without running
+        any step (the capture is then outside the advance)."""
+        with torch.cuda.device(self.device):
+            _lib.check(self._lib.his_engine_prepare(self._engine, int(n_steps)), "his_engine_prepare")
+
     def reports(self):
         reps = (_lib.MemberReport * self.B)()
         with torch.cuda.device(self.device):

@@ -24,8 +24,16 @@ COMPRESSED_SUFFIX = ".pt.gz"
 FORCING_STEPS = 64
 
 
-def record_path(root: Path, sim_id: int, compress: bool = True) -> Path:
-    return Path(root) / f"sim_{sim_id:05d}{COMPRESSED_SUFFIX if compress else '.pt'}"
+def record_path(root: Path, sim_id: int, compress: bool | None = None) -> Path:
+    """Path of record ``sim_id`` under ``root`` (hydrointel/data/generate.py:37).
+    compress True / False picks the gzip or the plain file; None (default) picks the
+    gzip file only when it exists and the plain one does not, so a directory of plain
+    records resolves to its own files."""
+    root = Path(root)
+    plain, packed = root / f"sim_{sim_id:05d}.pt", root / f"sim_{sim_id:05d}{COMPRESSED_SUFFIX}"
+    if compress is None:
+        return packed if packed.exists() and not plain.exists() else plain
+    return packed if compress else plain
 
 
 def save_record(rec: dict, path: Path) -> None:

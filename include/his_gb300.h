@@ -137,8 +137,10 @@ int32_t his_grid_volumes(his_grid* grid, double* vols, void* stream);
  * partial sums and tables live in a fixed library array of HIS_NOALLOC_SCRATCH_BYTES
  * bytes.  Same kernels, decomposition and results as a one-member grid set created
  * with default tiles.  Grids too large for the array return HIS_ERR_BAD_ARG.  The first
- * call on each device (with it current) looks up the array's address and should come
- * before any stream capture.  Calls share the array: calls that may overlap on the GPU
+ * call in each CUDA context (the device's primary context, or one the application made
+ * current itself; a context made after cudaDeviceReset counts as new) looks up the
+ * array's address in that context and should come before any stream capture.  Calls
+ * share the array: calls that may overlap on the GPU
  * (two streams, two threads) race on it; order them on one stream.  If vols is
  * non-NULL it receives the 5 float64 volumes of his_grid_step and the call
  * synchronises `stream`.
@@ -288,6 +290,14 @@ int32_t his_engine_destroy(his_engine* engine);
  * members run as independent chains (his_engine_set_chains), each on its own streams
  * and graphs; they join `stream` at the end of the call. */
 int32_t his_engine_advance(his_engine* engine, int32_t n_steps, void* stream);
+
+/* Capture, without running them, the CUDA graphs an advance of n_steps steps
+ * launches: one graph of graph_steps steps per chain and one of the remaining
+ * n_steps % graph_steps steps (one remainder size is kept at a time; an advance with
+ * another remainder captures anew).  his_engine_advance captures what is missing
+ * itself; calling this first keeps the capture out of a timed or latency-critical
+ * advance.  No reference counterpart (the reference has no graphs). */
+int32_t his_engine_prepare(his_engine* engine, int32_t n_steps);
 
 /* Split the members into n_chains (1..8, at most one per member) independent chains
  * of about equal 2-D work, each advanced on its own streams and CUDA graphs, so that

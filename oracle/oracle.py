@@ -329,6 +329,10 @@ class OracleCoupled:
         self.two, self.one, self.links, self.cfg = two, one, links, cfg
         self.rain = rain or (lambda t: 0.0)
         self.acc = {k: np.zeros(two.B) for k in TERMS}
+        # exchanged volume per member, 2-D -> 1-D and 1-D -> 2-D, and the links that moved
+        # water at least once (diagnostics: which parts of the coupling a run exercised)
+        self.exch = np.zeros((two.B, 2))
+        self.links_active = np.zeros((two.B, links.n_links if links is not None else 0), dtype=bool)
         self.v0 = self.total_volume()
         self.steps = 0
 
@@ -344,7 +348,10 @@ class OracleCoupled:
         if one is not None:
             if n_sub is None:
                 n_sub = max(1, math.ceil(dt / one.max_dt() - 1e-9))
-            exchange(one, two, self.links, dt)
+            V = exchange(one, two, self.links, dt)
+            self.exch[:, 0] += np.where(V > 0, V, 0.0).sum(axis=1)
+            self.exch[:, 1] += np.where(V < 0, -V, 0.0).sum(axis=1)
+            self.links_active |= V != 0
         vol = two.step(dt, t, self.rain(t))
         a = self.acc
         a["rain"] += vol["rain"]; a["infiltration"] += vol["infil"]; a["clip"] += vol["clip"]

@@ -58,3 +58,16 @@ def test_records_round_trip_with_index(tmp_path):
     assert rec["meta"]["key"] == "rec/1" and rec["h"].shape[0] == 4
     write_records([(storms[0], _result(storms[0]))], tmp_path, store_factor=1, compress=False, first_id=9)
     assert (tmp_path / "sim_00009.pt").exists() and len(json.loads(idx.read_text())) == 3
+
+
+def test_record_path_default_resolves_to_the_existing_file(tmp_path):
+    """compress=None: the plain .pt file unless only the gzip file exists (the reference's
+    record lookup, hydrointel/data/generate.py:37-43); explicit True / False choose."""
+    from his_gb300.records import record_path
+    assert record_path(tmp_path, 3).name == "sim_00003.pt"
+    (tmp_path / "sim_00003.pt.gz").write_bytes(b"")
+    assert record_path(tmp_path, 3).name == "sim_00003.pt.gz"
+    (tmp_path / "sim_00003.pt").write_bytes(b"")
+    assert record_path(tmp_path, 3).name == "sim_00003.pt"
+    assert record_path(tmp_path, 3, compress=True).name == "sim_00003.pt.gz"
+    assert record_path(tmp_path, 3, compress=False).name == "sim_00003.pt"

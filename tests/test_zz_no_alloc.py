@@ -1,9 +1,10 @@
 """The allocation-free 2-D step (his_grid_step_noalloc) against his_grid_step.
 
 Both entry points run the same strip kernels on the same decomposition (58-column
-strips, 48-row chunks), so a grid stepped through the scratch compiled into the
-library must match a one-member grid set stepped through its own allocated scratch,
-call after call, within the parity tolerances of the float64 and float32 paths.
+strips, 48-row chunks) and sum the volume partials in the same fixed order, so a grid
+stepped through the scratch compiled into the library must equal a one-member grid set
+stepped through its own allocated scratch bit for bit, call after call, in both
+precisions.
 This file sorts last so that the shared scratch has been through every other test's
 process state first; it passes alone as well.
 """
@@ -18,8 +19,6 @@ from his_gb300.boundaries import EdgeBC
 from his_gb300.config import SolverConfig
 from his_gb300.infiltration import Horton
 
-STATE_TOL = {torch.float64: 1e-12, torch.float32: 2e-6}
-VOL_REL = {torch.float64: 1e-11, torch.float32: 1e-5}
 FIELDS = ("h", "hu", "hv", "s_filled", "infil_cum")
 
 
@@ -73,16 +72,13 @@ class Twin:
         return dt, want, got
 
     def compare(self, want, got, k):
-        dtype = self.sim.dtype
         ref = np.array([float(getattr(want, f)) for f in ("bnd_in", "bnd_out", "rain", "infil", "clip")])
-        scale = max(float(np.abs(ref).max()), 1e-9)
-        assert np.max(np.abs(got - ref)) <= VOL_REL[dtype] * scale + 1e-13, f"call {k}: volumes {got} vs {ref}"
+        assert np.array_equal(got, ref), f"call {k}: volumes {got} vs {ref}"
         for f in FIELDS:
-            a = self.state[f].double()
-            b = getattr(self.sim, f).double()
+            a = self.state[f]
+            b = getattr(self.sim, f)
             assert torch.isfinite(a).all(), f"call {k}: {f} not finite"
-            err = float((a - b).abs().max())
-            assert err <= STATE_TOL[dtype], f"call {k}: {f} differs by {err}"
+            assert torch.equal(a, b), f"call {k}: {f} differs by {float((a.double() - b.double()).abs().max())}"
 
 
 @pytest.mark.gpu
@@ -102,6 +98,52 @@ def test_noalloc_step_matches_grid_step_two_calls_in_a_row(dtype, order):
         large.compare(want, got, k)
         t_large += dt
     assert float(large.state["h"].double().sum()) > 0.0
+
+
+NPART = 16                       # float64 partial sums per strip-chunk
+STRIP_REF_BYTES = 24             # one strip-chunk record
+
+
+def _plan_bytes(ny, nx, elem):
+    """Scratch a grid needs: three stage planes, the partial sums and strip records of
+    its 58-column x 48-row strip-chunks, and three 256-byte record slots, each region
+    rounded up to 256 bytes."""
+    a = lambda x: (x + 255) // 256 * 256
+    n = -(-nx // 58) * -(-ny // 48)
+    return 3 * a(ny * nx * elem) + a(8 * NPART * n) + a(STRIP_REF_BYTES * n) + 3 * 256
+
+
+def _call_noalloc(prec, ny, nx, dt):
+    """his_grid_step_noalloc on a grid of fake addresses: every argument check runs, and
+    the call is rejected before any device work (dt = NaN fails the last check)."""
+    lib = _lib.load()
+    cfg = _lib.solver_cfg(SolverConfig())
+    d = _lib.GridDesc()
+    d.ny, d.nx = ny, nx
+    d.dx = d.dy = 10.0
+    for name in ("h", "hu", "hv", "s_filled", "infil_cum", "z", "manning"):
+        setattr(d, name, 0x1000)                       # never dereferenced: rejected before any device work
+    params = _lib.StepParams()
+    params.dt = dt
+    rc = lib.his_grid_step_noalloc(prec, C.byref(cfg), C.byref(d), C.byref(params), None, None)
+    return rc, _lib.last_error()
+
+
+@pytest.mark.parametrize("prec,elem", [(_lib.PREC_F64, 8), (_lib.PREC_F32, 4)], ids=["f64", "f32"])
+def test_noalloc_accepts_up_to_its_scratch_size_exactly(prec, elem):
+    """At the largest accepted grid (for a 600-row and a 1-row shape) the size checks pass
+    and the NaN dt is what is rejected; one column more and the size is rejected."""
+    for ny in (600, 1):
+        lo, hi = 1, _lib.NOALLOC_SCRATCH_BYTES          # fits at lo, not at hi
+        while hi - lo > 1:
+            mid = (lo + hi) // 2
+            lo, hi = (mid, hi) if _plan_bytes(ny, mid, elem) <= _lib.NOALLOC_SCRATCH_BYTES else (lo, mid)
+        nx = lo
+        assert _plan_bytes(ny, nx, elem) <= _lib.NOALLOC_SCRATCH_BYTES < _plan_bytes(ny, nx + 1, elem)
+        rc, msg = _call_noalloc(prec, ny, nx, float("nan"))
+        assert rc == _lib.HIS_ERR_BAD_ARG and "finite" in msg, (ny, nx, msg)
+        rc, msg = _call_noalloc(prec, ny, nx + 1, float("nan"))
+        assert rc == _lib.HIS_ERR_BAD_ARG and "scratch" in msg, (ny, nx + 1, msg)
 
 
 def test_noalloc_rejects_a_grid_beyond_its_scratch_without_a_gpu():
