@@ -7,7 +7,7 @@ or ``("junction", j)``.  This is the input format of the 1-D network kernel.
 """
 from __future__ import annotations
 
-import copy
+import dataclasses
 from dataclasses import dataclass, field
 
 import numpy as np
@@ -68,40 +68,59 @@ class ChannelNetwork:
     def n_reaches(self) -> int:
         return len(self.reaches)
 
-    def validate(self) -> None:
+    def problems(self):
+        """Yield a message for every rule the network breaks: per-node fields of each
+        reach with the node count and finite; positive width and roughness, side
+        slopes >= 0; bank crest >= bed + 0.2 m; reach ends of a known kind, naming an
+        existing junction (hydrointel/domain/channels.py:77-94)."""
+        end_kinds = ("inflow", "stage", "closed", "junction")
         for r in self.reaches:
-            for name in ("bed", "width", "side_slope", "manning", "z_bank"):
-                a = np.asarray(getattr(r, name))
-                if a.shape != np.asarray(r.x).shape or not np.all(np.isfinite(a)):
-                    raise ValueError(f"reach {r.reach_id}: field '{name}' has bad shape or non-finite values")
-            if np.any(r.width <= 0) or np.any(r.side_slope < 0) or np.any(r.manning <= 0):
-                raise ValueError(f"reach {r.reach_id}: width/manning must be > 0 and side_slope >= 0")
-            if np.any(r.z_bank - r.bed < 0.2):
-                raise ValueError(f"reach {r.reach_id}: bank crest must be at least 0.2 m above bed")
+            nodes = np.shape(r.x)
+            fields = {name: np.asarray(getattr(r, name), dtype=float) for name in _NODE_FIELDS}
+            broken = [n for n, a in fields.items() if a.shape != nodes or not np.isfinite(a).all()]
+            for name in broken:
+                yield f"reach {r.reach_id}: field '{name}' has bad shape or non-finite values"
+            if broken:
+                continue
+            if (fields["width"] <= 0).any() or (fields["manning"] <= 0).any() or (fields["side_slope"] < 0).any():
+                yield f"reach {r.reach_id}: width/manning must be > 0 and side_slope >= 0"
+            if ((fields["z_bank"] - fields["bed"]) < 0.2).any():
+                yield f"reach {r.reach_id}: bank crest must be at least 0.2 m above bed"
             for end in (r.up, r.down):
-                if end[0] not in ("inflow", "stage", "closed", "junction"):
-                    raise ValueError(f"reach {r.reach_id}: unknown boundary kind {end[0]}")
-                if end[0] == "junction" and not 0 <= end[1] < len(self.junctions):
-                    raise ValueError(f"reach {r.reach_id}: junction index {end[1]} out of range")
+                if end[0] not in end_kinds:
+                    yield f"reach {r.reach_id}: unknown boundary kind {end[0]}"
+                elif end[0] == "junction" and not 0 <= end[1] < len(self.junctions):
+                    yield f"reach {r.reach_id}: junction index {end[1]} out of range"
+
+    def validate(self) -> None:
+        """Raise ValueError with the first problem found (``problems``)."""
+        for msg in self.problems():
+            raise ValueError(msg)
+
+
+_NODE_FIELDS = ("bed", "width", "side_slope", "manning", "z_bank")
 
 
 def apply_gamma(net: ChannelNetwork, gamma) -> ChannelNetwork:
-    """Per-reach conveyance scale: bottom width and bankfull depth both times sqrt(gamma),
-    the bed moved about the fixed bank crest; a junction takes the factor of each reach
-    that ends at it."""
+    """A copy of ``net`` with each reach's conveyance scaled by its gamma: with
+    s = sqrt(gamma), the bottom width becomes s times wider and the depth below the
+    fixed bank crest s times deeper, so a rectangular bankfull area scales by gamma
+    while the 2-D terrain is untouched.  A junction is rescaled the same way by every
+    reach that ends at it, in reach order (hydrointel/domain/channels.py:172-193)."""
     g = np.asarray(gamma, dtype=float).reshape(-1)
     if g.size != net.n_reaches:
         raise ValueError(f"channel_gamma has {g.size} entries, network has {net.n_reaches} reaches")
-    if np.any(g <= 0):
+    if (g <= 0).any():
         raise ValueError("channel_gamma must be positive")
-    out = copy.deepcopy(net)
-    for r, gi in zip(out.reaches, g):
-        s = np.sqrt(gi)
-        r.width = r.width * s
-        r.bed = r.z_bank - (r.z_bank - r.bed) * s
+    s = np.sqrt(g)
+    deepen = lambda crest, bed, f: crest - (crest - bed) * f
+    reaches = [dataclasses.replace(r, width=r.width * f, bed=deepen(r.z_bank, r.bed, f))
+               for r, f in zip(net.reaches, s)]
+    junctions = [dataclasses.replace(j) for j in net.junctions]
+    for r, f in zip(net.reaches, s):
         if r.down[0] == "junction":
-            j = out.junctions[r.down[1]]
-            j.width *= s
-            j.bed = j.z_bank - (j.z_bank - j.bed) * s
+            j = junctions[r.down[1]]
+            j.width, j.bed = j.width * f, deepen(j.z_bank, j.bed, f)
+    out = ChannelNetwork(reaches, junctions, net.inflow_reach)
     out.validate()
     return out

@@ -180,29 +180,40 @@ class CoupledEngine:
         # state version of the 1-D model when its rates were last reduced ahead (None: not)
         self._rates1_at = None
 
+    def plausibility(self) -> np.ndarray:
+        """Per member (rows): the largest 2-D depth and the highest 1-D water level above
+        its bank crest over interior cells (NaN where a model is absent), reduced on the
+        device and copied to the host in one transfer."""
+        two, one = self.two, self.one
+        cols = [two.h.reshape(two.B, -1).amax(dim=1).double()]
+        if one is not None:
+            above = one.z + one.sec.depth(one.A) - torch.as_tensor(one.topo.zbank, dtype=one.A.dtype,
+                                                                  device=one.A.device)
+            above = torch.where(one.interior, above, torch.full_like(above, -math.inf)).reshape(one.B, -1)
+            cols.append(above.amax(dim=1).double().to(two.device))
+        stats = torch.stack(cols, dim=1).cpu().numpy()
+        if one is None:
+            stats = np.concatenate([stats, np.full((two.B, 1), np.nan)], axis=1)
+        return stats
+
     def check_plausible(self, t: float, label: str = "") -> None:
-        h = self.two.h
-        dmax = h.flatten(-2).amax(-1) if h.dim() == 3 else h.max()
-        bad2 = ~torch.isfinite(dmax) | (dmax > MAX_PLAUSIBLE_DEPTH_2D_M)
-        bad1 = torch.zeros_like(bad2)
-        rise = None
+        """Raise NumericalInstabilityError naming every member whose state left the
+        physically possible range: a non-finite or deeper than 10 m 2-D cell, or a 1-D
+        level non-finite or more than 10 m above the bank (coupling.py:169-192)."""
+        stats = self.plausibility()
+        limits = np.array([MAX_PLAUSIBLE_DEPTH_2D_M, MAX_PLAUSIBLE_RISE_1D_M])
+        broken = np.isnan(stats[:, 0]) | np.isinf(stats[:, 0]) | (stats[:, 0] > limits[0])
         if self.one is not None:
-            one = self.one
-            level = one.z + one.sec.depth(one.A)
-            zb = torch.as_tensor(one.topo.zbank, dtype=level.dtype, device=level.device)
-            rise = torch.where(one.interior, level - zb, torch.full_like(level, -1e9)).amax(-1)
-            bad1 = (~torch.isfinite(rise) | (rise > MAX_PLAUSIBLE_RISE_1D_M)).to(bad2.device)
-        bad = (bad2 | bad1).reshape(-1)
-        if bool(bad.any()):
-            members = torch.nonzero(bad).reshape(-1).tolist()
-            d2 = dmax.reshape(-1).tolist()
-            d1 = rise.reshape(-1).tolist() if rise is not None else [float("nan")] * len(d2)
-            who = ", ".join(f"member {m}: max 2-D depth {d2[m]:.2f} m, max 1-D rise above bank {d1[m]:.2f} m"
-                            for m in members) if self.batch is not None else \
-                f"max 2-D depth {d2[0]:.2f} m, max 1-D rise above bank {d1[0]:.2f} m"
-            raise NumericalInstabilityError(
-                f"physically impossible state{(' in ' + label) if label else ''} at t = {t / 3600:.3f} h ({who}; "
-                f"bounds {MAX_PLAUSIBLE_DEPTH_2D_M:g} m and {MAX_PLAUSIBLE_RISE_1D_M:g} m). The run is invalid.")
+            broken |= ~np.isfinite(stats[:, 1]) | (stats[:, 1] > limits[1])
+        if not broken.any():
+            return
+        fmt = lambda m: (f"{'member %d: ' % m if self.batch is not None else ''}max 2-D depth {stats[m, 0]:.2f} m, "
+                         f"max 1-D rise above bank {stats[m, 1]:.2f} m")
+        where = f" in {label}" if label else ""
+        raise NumericalInstabilityError(
+            f"physically impossible state{where} at t = {t / 3600:.3f} h "
+            f"({', '.join(fmt(int(m)) for m in np.flatnonzero(broken))}; bounds {limits[0]:g} m and "
+            f"{limits[1]:g} m). The run is invalid.")
 
     def total_volume(self):
         v = self.two.volume() + self.two.storage_volume()
@@ -277,54 +288,112 @@ class CoupledEngine:
         return t + dt
 
     def snapshot(self, t: float) -> Snapshot:
-        two = self.two
+        """The state at ``t`` as host float32 arrays (depth, KP velocities, 1-D level and
+        discharge) and the volume ledger (2-D surface, 1-D channel and retained water
+        plus the accumulated terms), gathered with non-blocking copies into pinned
+        memory and one wait (coupling.py:229-242)."""
+        two, one = self.two, self.one
         u, v = two.velocities(two.h, two.hu, two.hv)
-        cast = lambda a: a.to(torch.float32).cpu().numpy()
-        if self.one is not None:
-            eta1, q1 = cast(self.one.level()), cast(self.one.Q)
-        else:
-            eta1 = q1 = np.zeros(0, np.float32)
-        src = self.mb.sources()
-        num = (lambda x: x.detach().cpu().numpy()) if self.batch is not None else float
-        ledger = {"v2d": num(two.volume()), "v1d": num(self.one.volume()) if self.one is not None else 0.0,
-                  "storage": num(two.storage_volume()), **src}
-        return Snapshot(t, cast(two.h), cast(u), cast(v), eta1, q1, ledger)
+        parts = {"h": two.h, "u": u, "v": v}
+        if one is not None:
+            parts.update(eta1=one.level(), q1=one.Q)
+        vols = {"v2d": two.volume(), "storage": two.storage_volume()}
+        if one is not None:
+            vols["v1d"] = one.volume()
+        host = {}
+        for name, x in list(parts.items()) + list(vols.items()):
+            dt = torch.float64 if name in vols else torch.float32
+            dst = torch.empty(x.shape, dtype=dt, pin_memory=True)
+            dst.copy_(x.detach().to(dt), non_blocking=True)
+            host[name] = dst
+        torch.cuda.current_stream(two.device).synchronize()
+        as_num = (lambda a: a.numpy()) if self.batch is not None else (lambda a: float(a))
+        ledger = {"v2d": as_num(host["v2d"]), "v1d": as_num(host["v1d"]) if one is not None else 0.0,
+                  "storage": as_num(host["storage"])}
+        ledger.update(self.mb.sources())
+        empty = np.zeros(0, np.float32)
+        return Snapshot(t, host["h"].numpy(), host["u"].numpy(), host["v"].numpy(),
+                        host["eta1"].numpy() if one is not None else empty,
+                        host["q1"].numpy() if one is not None else empty, ledger)
 
     def run(self, t_end: float, out_times=(), t0: float = 0.0, on_snapshot=None, check_every: int = 500,
             label: str = "", progress_s: float = 120.0):
-        wall = time.perf_counter()
-        last_report = wall
+        """Advance from t0 to t_end; each requested output time cuts a step and, with
+        ``on_snapshot``, hands it the snapshot there.  The state is checked for
+        plausibility at every output and every ``check_every`` steps (when the mass
+        series also gets an entry), and at the end, where the mass balance must hold
+        to cfg.mass_tol; returns the final relative mass errors (coupling.py:244-286).
+        Every ``progress_s`` s of wall time a progress line is logged."""
+        clock0 = time.perf_counter()
+        schedule = _OutputSchedule(out_times, t0, t_end)
+        report = _Progress(label, t0, t_end, progress_s)
         t = t0
-        outs = sorted(float(x) for x in out_times if t0 <= x <= t_end + 1e-9)
-        k = 0
-        if outs and abs(outs[0] - t0) < 1e-9:
-            on_snapshot and on_snapshot(self.snapshot(t0))
-            outs.pop(0)
+        if schedule.due(t0) and on_snapshot is not None:
+            on_snapshot(self.snapshot(t0))
+        if schedule.due(t0):
+            schedule.advance()
+        n = 0
         while t < t_end - 1e-9:
-            limit = outs[0] if outs else t_end
-            t = self.step(t, limit)
-            if outs and t >= outs[0] - 1e-9:
+            t = self.step(t, schedule.limit(t_end))
+            n += 1
+            at_output = schedule.due(t)
+            periodic = n % check_every == 0
+            if at_output or periodic:
                 self.check_plausible(t, label)
-                on_snapshot and on_snapshot(self.snapshot(t))
-                outs.pop(0)
-            k += 1
-            if k % check_every == 0:
+            if at_output:
+                if on_snapshot is not None:
+                    on_snapshot(self.snapshot(t))
+                schedule.advance()
+            if periodic:
                 self.mb.check(self.total_volume(), t)
-                self.check_plausible(t, label)
-            if progress_s and time.perf_counter() - last_report >= progress_s:
-                last_report = time.perf_counter()
-                done = (t - t0) / (t_end - t0) if t_end > t0 else 1.0
-                log.info("%s%.1f%% of %.2f h: t = %.2f h, %d steps", f"{label}: " if label else "", 100 * done,
-                         (t_end - t0) / 3600, t / 3600, self.log.steps)
-        self.log.wall_s += time.perf_counter() - wall
+            report.maybe(t, self.log)
+        self.log.wall_s += time.perf_counter() - clock0
         if self.links is not None:
-            ex = self.links.exchanged()
-            num = (lambda x: x) if self.batch is not None else (lambda x: float(x[0]))
-            self.log.exchanged_in_m3 = num(ex[:, 0])
-            self.log.exchanged_out_m3 = num(ex[:, 1])
+            totals = self.links.exchanged()
+            pick = (lambda col: totals[:, col]) if self.batch is not None else (lambda col: float(totals[0, col]))
+            self.log.exchanged_in_m3, self.log.exchanged_out_m3 = pick(0), pick(1)
         self.log.n_dt_clamped = self.two.n_dt_clamped
         self.check_plausible(t, label)
         return self.mb.assert_ok(self.total_volume(), t, self.cfg.mass_tol, label)
+
+
+class _OutputSchedule:
+    """Requested output times within [t0, t_end], in order; the next one limits a step."""
+
+    def __init__(self, times, t0: float, t_end: float):
+        self._times = sorted(float(x) for x in times if t0 <= x <= t_end + 1e-9)
+        self._k = 0
+
+    def due(self, t: float) -> bool:
+        return self._k < len(self._times) and t >= self._times[self._k] - 1e-9
+
+    def advance(self) -> None:
+        self._k += 1
+
+    def limit(self, t_end: float) -> float:
+        return self._times[self._k] if self._k < len(self._times) else t_end
+
+
+class _Progress:
+    """Logs how far a long run has got, at most every ``period`` s of wall time."""
+
+    def __init__(self, label: str, t0: float, t_end: float, period: float):
+        self.prefix = f"{label}: " if label else ""
+        self.t0, self.span, self.period = t0, t_end - t0, period
+        self.start = self.last = time.perf_counter()
+
+    def maybe(self, t: float, runlog) -> None:
+        if not self.period:
+            return
+        now = time.perf_counter()
+        if now - self.last < self.period:
+            return
+        self.last = now
+        frac = (t - self.t0) / self.span if self.span > 0 else 1.0
+        spent = now - self.start
+        left = spent * (1.0 - frac) / frac if frac > 0 else float("nan")
+        log.info("%s%.1f%% of %.2f h simulated (t = %.2f h) after %d steps and %.0f s; about %.0f s to go",
+                 self.prefix, 100.0 * frac, self.span / 3600.0, t / 3600.0, runlog.steps, spent, left)
 
 
 __all__ = ["Links", "build_links", "links_from_cells", "exchange", "CoupledEngine", "Snapshot", "RunLog",

@@ -1,124 +1,154 @@
-"""Per-member volume accounting, with the reference's terms, error measure and
-messages (hydrointel/solver/massbalance.py:18-77).
+"""Per-member volume accounting of the coupled engine.
 
-relative_error = |dV - net| / max(gross, 1e-9 |V0| + 1), where dV counts 2-D
-surface water, retained (stored) water and 1-D channel water, net = rain -
-infiltration + boundary in - boundary out (2-D and 1-D), gross is the sum of their
-magnitudes, and ``clip`` (volume created by clamping negative depths) is an error
-term, not a source.
+Contract kept from the reference (hydrointel/solver/massbalance.py:18-77): the class
+name and constructor ``MassBalance(device, v0)``, the seven term names, ``add``,
+``sources``, ``check`` and ``assert_ok``, the error measure
 
-The accumulators live wherever the caller keeps them: the device-resident engine
-accumulates on the GPU in float64 and hands this class host copies; the drop-in
-classes ``add`` one step at a time, as the reference does.
+    relative_error = |dV - net| / max(gross, 1e-9 |V0| + 1)
+
+(dV: change of 2-D surface + retained + 1-D channel water; net: the signed sources;
+gross: their magnitudes; ``clip``, the volume created by clamping negative depths,
+is an error term and enters neither), the ``mass_series`` record keys that
+hydrointel/api.py reads, and ``AssertionError("mass balance violated ...")`` naming
+the failing members.
+
+Design: every term lives in one float64 ledger of shape (7, n) per device (n = batch
+size, 1 unbatched), so adding a step's terms is one device operation and nothing is
+copied to the host until ``sources`` or ``check`` is called.  Net and gross are a dot
+product of the ledger with fixed sign and weight vectors.  The device-resident engine
+keeps its own float64 ledger on the GPU and hands totals in through ``set_totals``.
 """
 from __future__ import annotations
 
 import numpy as np
 
 TERMS = ("rain", "infiltration", "bnd2d_in", "bnd2d_out", "bnd1d_in", "bnd1d_out", "clip")
+_ROW = {name: i for i, name in enumerate(TERMS)}
+# contribution of each term to the net source (+ into the water body, - out of it) and
+# to the gross turnover; clip counts in neither
+NET_SIGN = np.array([1.0, -1.0, 1.0, -1.0, 1.0, -1.0, 0.0])
+GROSS_WEIGHT = np.abs(NET_SIGN)
 
 
-def _np(v):
+def _host(v) -> np.ndarray:
     if hasattr(v, "detach"):
-        return v.detach().to("cpu").double().numpy()
-    return v
+        v = v.detach().to("cpu").double().numpy()
+    return np.asarray(v, dtype=np.float64)
+
+
+def relative_error(ledger: np.ndarray, volume_now, v0) -> tuple[np.ndarray, np.ndarray, np.ndarray]:
+    """(error, net, gross) per member from a (7, n) ledger, the current and the initial
+    volume (arrays of n)."""
+    net = NET_SIGN @ ledger
+    gross = GROSS_WEIGHT @ ledger
+    floor = 1e-9 * np.abs(v0) + 1.0
+    return np.abs((volume_now - v0) - net) / np.maximum(gross, floor), net, gross
 
 
 class MassBalance:
     def __init__(self, device, v0):
         self.device = device
-        self.v0 = np.asarray(_np(v0), dtype=np.float64)
-        self.batch = self.v0.shape[0] if self.v0.ndim else None
-        self.acc: dict[tuple[str, str], object] = {}
+        v0 = _host(v0)
+        self.batch = int(v0.shape[0]) if v0.ndim else None
+        self.v0 = v0
+        self._n = self.batch or 1
+        self._ledgers: dict[str, object] = {}     # device name -> (7, n) float64 tensor
+        self._index_cache: dict = {}
         self.series: list[dict] = []
 
-    def add(self, name: str, value) -> None:
+    # ------------------------------------------------------------------ adding
+    def _ledger(self, device):
         import torch
-        if name not in TERMS:
+        key = str(device)
+        led = self._ledgers.get(key)
+        if led is None:
+            led = self._ledgers[key] = torch.zeros((len(TERMS), self._n), dtype=torch.float64, device=device)
+        return led
+
+    def add(self, name: str, value) -> None:
+        """Accumulate one term for this step: a float64 scalar (every member) or one
+        value per member, on any device."""
+        import torch
+        row = _ROW.get(name)
+        if row is None:
             raise KeyError(name)
-        if not torch.is_tensor(value):
-            value = torch.tensor(np.asarray(value, dtype=np.float64), dtype=torch.float64)
-        value = value.to(torch.float64)
-        if self.batch is not None and value.dim() == 0:
-            value = value.expand(self.batch)
-        if tuple(value.shape) != self.v0.shape:
-            raise ValueError(f"mass term '{name}' has shape {tuple(value.shape)}, expected {self.v0.shape}")
-        key = (name, str(value.device))
-        if key not in self.acc:
-            self.acc[key] = torch.zeros_like(value)
-        self.acc[key] += value
+        v = value if torch.is_tensor(value) else torch.as_tensor(np.asarray(value, dtype=np.float64))
+        v = v.to(torch.float64)
+        want = (self.batch,) if self.batch is not None else ()
+        if v.dim() and tuple(v.shape) != want:
+            raise ValueError(f"mass term '{name}' has shape {tuple(v.shape)}, expected {want}")
+        led = self._ledger(v.device)
+        led[row] += v.reshape(-1) if v.dim() else v
 
     def add_columns(self, names: tuple, values) -> None:
-        """Add the columns of ``values`` (B x len(names) float64 device tensor) to the
-        named terms in one device operation.  Each term receives the same float64 sums
-        as ``add`` one column at a time (every index is distinct, so each accumulator
-        element gets exactly one addition per call)."""
+        """Accumulate several terms at once from the columns of ``values`` (n x
+        len(names), float64, on the device that produced them): one index_add into
+        the ledger, the same float64 sums as adding the columns one by one (each
+        ledger element receives one addition per call)."""
         import torch
-        cache = self.__dict__.setdefault("_col_idx", {})
-        idx = cache.get((names, values.device))
+        idx = self._index_cache.get((names, values.device))
         if idx is None:
-            for n in names:
-                if n not in TERMS:
-                    raise KeyError(n)
+            unknown = [n for n in names if n not in _ROW]
+            if unknown:
+                raise KeyError(unknown[0])
             if len(set(names)) != len(names):
                 raise ValueError("a term may appear once per add_columns call")
-            idx = cache[(names, values.device)] = torch.as_tensor([TERMS.index(n) for n in names],
-                                                                   device=values.device)
-        B = self.v0.size
-        if tuple(values.shape) != (B, len(names)):
-            raise ValueError(f"mass columns have shape {tuple(values.shape)}, expected ({B}, {len(names)})")
-        key = ("_columns", str(values.device))
-        acc = self.acc.get(key)
-        if acc is None:
-            acc = self.acc[key] = torch.zeros((len(TERMS), B), dtype=torch.float64, device=values.device)
-        acc.index_add_(0, idx, values.t().to(torch.float64))
+            idx = torch.as_tensor([_ROW[n] for n in names], device=values.device)
+            self._index_cache[(names, values.device)] = idx
+        if tuple(values.shape) != (self._n, len(names)):
+            raise ValueError(f"mass columns have shape {tuple(values.shape)}, expected ({self._n}, {len(names)})")
+        self._ledger(values.device).index_add_(0, idx, values.t().to(torch.float64))
 
     def set_totals(self, totals: dict) -> None:
-        """Replace the accumulators by totals computed elsewhere (e.g. on the device)."""
+        """Replace the ledger by totals accumulated elsewhere (e.g. on the device)."""
         import torch
-        self.acc = {}
-        for k, v in totals.items():
-            if k not in TERMS:
-                raise KeyError(k)
-            t = torch.as_tensor(np.asarray(v, dtype=np.float64).reshape(self.v0.shape), dtype=torch.float64)
-            self.acc[(k, "cpu")] = t
+        led = np.zeros((len(TERMS), self._n))
+        for name, v in totals.items():
+            if name not in _ROW:
+                raise KeyError(name)
+            led[_ROW[name]] = _host(v).reshape(self._n)
+        self._ledgers = {"cpu": torch.as_tensor(led)}
+
+    # ---------------------------------------------------------------- reading
+    def ledger(self) -> np.ndarray:
+        """All terms as a host (7, n) float64 array (ledgers of several devices summed)."""
+        total = np.zeros((len(TERMS), self._n))
+        for led in self._ledgers.values():
+            total += _host(led)
+        return total
 
     def sources(self) -> dict:
-        zero = np.zeros(self.v0.shape)
-        out = {k: zero.copy() for k in TERMS}
-        for (k, _), v in self.acc.items():
-            if k == "_columns":
-                cols = _np(v)
-                for i, name in enumerate(TERMS):
-                    out[name] = out[name] + cols[i].reshape(self.v0.shape)
-                continue
-            out[k] = out[k] + _np(v)
-        return {k: (v if self.batch is not None else float(v)) for k, v in out.items()}
+        """Accumulated volume per term: floats unbatched, arrays of the members batched."""
+        led = self.ledger()
+        if self.batch is None:
+            return {name: float(led[i, 0]) for i, name in enumerate(TERMS)}
+        return {name: led[i].copy() for i, name in enumerate(TERMS)}
 
     def check(self, volume_now, t: float, record: bool = True):
-        s = self.sources()
-        net = s["rain"] - s["infiltration"] + s["bnd2d_in"] - s["bnd2d_out"] + s["bnd1d_in"] - s["bnd1d_out"]
-        gross = s["rain"] + s["infiltration"] + s["bnd2d_in"] + s["bnd2d_out"] + s["bnd1d_in"] + s["bnd1d_out"]
-        dv = np.asarray(_np(volume_now), dtype=np.float64) - self.v0
-        err = np.abs(dv - net) / np.maximum(gross, 1e-9 * np.abs(self.v0) + 1.0)
+        """Relative error per member now; ``record`` appends a mass-series entry."""
+        led = self.ledger()
+        vol = _host(volume_now).reshape(self._n)
+        err, net, gross = relative_error(led, vol, self.v0.reshape(self._n))
+        scalar = self.batch is None
+        out = (lambda a: float(a[0])) if scalar else (lambda a: a)
         if record:
-            f = (lambda x: x) if self.batch is not None else float
-            self.series.append({"t": t, "volume": f(_np(volume_now)), "net_sources": f(net), "gross": f(gross),
-                                "clip": f(s["clip"]), "rel_error": f(err)})
-        return err if self.batch is not None else float(err)
+            self.series.append({"t": t, "volume": out(vol), "net_sources": out(net), "gross": out(gross),
+                                "clip": out(led[_ROW["clip"]]), "rel_error": out(err)})
+        return out(err)
 
     def assert_ok(self, volume_now, t: float, tol: float, label: str = ""):
+        """``check`` and raise AssertionError naming the members at or above ``tol``."""
         err = self.check(volume_now, t)
-        if self.batch is not None:
-            bad = np.nonzero(~(np.asarray(err) < tol))[0]
-        else:
-            bad = [] if err < tol else [0]
-        if len(bad):
-            where = f" in {label}" if label else ""
-            if self.batch is not None:
-                detail = ", ".join(f"member {int(i)}: {np.asarray(err)[int(i)]:.3e}" for i in bad[:8])
-                raise AssertionError(f"mass balance violated{where} for {len(bad)}/{self.batch} batch members "
-                                     f"(tolerance {tol:.1e}) -- {detail}")
+        failing = np.flatnonzero(~(np.atleast_1d(err) < tol))
+        if failing.size == 0:
+            return err
+        where = f" in {label}" if label else ""
+        if self.batch is None:
             raise AssertionError(f"mass balance violated{where}: relative error {float(err):.3e} >= {tol:.1e} "
                                  f"(sources {self.sources()})")
-        return err
+        named = ", ".join(f"member {int(m)}: {err[int(m)]:.3e}" for m in failing[:8])
+        raise AssertionError(f"mass balance violated{where} for {failing.size}/{self.batch} batch members "
+                             f"(tolerance {tol:.1e}) -- {named}")
+
+
+__all__ = ["MassBalance", "TERMS", "relative_error"]
