@@ -48,3 +48,16 @@ class SolverConfig:
 
     def to_dict(self) -> dict:
         return asdict(self)
+
+    @classmethod
+    def coerce(cls, cfg) -> "SolverConfig":
+        """This class from any object carrying the solver fields (the reference's own
+        SolverConfig, a RunConfig's ``solver``): every field found is copied, the
+        rest keep their defaults."""
+        if isinstance(cfg, cls):
+            return cfg
+        out = cls()
+        for name in out.__dataclass_fields__:
+            if hasattr(cfg, name):
+                setattr(out, name, getattr(cfg, name))
+        return out

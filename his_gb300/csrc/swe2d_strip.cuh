@@ -35,26 +35,27 @@ struct alignas(4 * sizeof(R)) Q4 {
     R a, b, c, d;
 };
 
-// Shared-memory layout of one CTA
+// Shared-memory layout of one CTA.  Only what a neighbouring thread reads lives here
+// (cells of the rows around the x-reconstruction, the plus side of each x-
+// reconstruction, x-faces and theta); a thread's own column -- its cells, y-faces,
+// thetas and bed terms -- is carried in registers from row to row.  Every array has
+// one padding slot on each side: thread t's entry is at t + 1, so the neighbours of
+// the first and last thread are in bounds (their values are never used).
 template <class R, int NT>
 struct StripGeom {
-    static constexpr int RING = 4;                 // cell rows kept (rows r-3 .. r are live)
-    static constexpr int FR = 4;                   // y-face and theta rows kept (3 live)
-    static constexpr int FRX = 2;                  // x-face rows kept (2 live)
+    static constexpr int RING = 4;                 // cell rows kept (rows r-2 .. r are read)
+    static constexpr int P = NT + 2;               // padded row of entries
     static constexpr int NRED = 11;                // reduced values (the reduction reuses the cell ring)
-    static constexpr size_t quads = (size_t)(RING + 2 + FRX + FR) * NT;
-    static constexpr size_t th = (size_t)FR * NT;
-    static_assert((size_t)4 * RING * NT >= (size_t)32 * NRED, "reduction scratch must fit in the cell ring");
-    static constexpr size_t smem_bytes = sizeof(Q4<R>) * quads + sizeof(R) * th;
-    // resident CTAs per SM the float32 kernels are register-capped for (shared memory
-    // allows 14 of 64 threads): about 768 threads' worth for stage 1 and 640 for the
-    // larger stage-2 body, so that they keep their live values in registers.  With the
-    // engine's member chains running side by side this beat tighter caps (896 / 768:
-    // 0.474 against 0.466 ms per step at 64 x 400 x 325) and looser ones (640 / 512:
-    // 0.502 ms).  float64 keeps the compiler's choice (one CTA of any width must fit
-    // the register file)
+    // cells [RING][P], x-recon plus side [P], x-faces [2][P]; then plus-side surface
+    // slope [P] and theta [2][P]
+    static constexpr size_t quads = (size_t)(RING + 1 + 2) * P;
+    static constexpr size_t scalars = (size_t)(1 + 2) * P;
+    static_assert((size_t)4 * RING * P >= (size_t)(NT / 32) * NRED, "reduction scratch must fit in the cell ring");
+    static constexpr size_t smem_bytes = sizeof(Q4<R>) * quads + sizeof(R) * scalars;
+    // resident CTAs per SM the float32 kernels are register-capped for; float64 keeps
+    // the compiler's choice (one CTA of any width must fit the register file)
     static constexpr int min_ctas(int stage) {
-        return sizeof(R) == 4 ? ((stage == 1 ? 768 : 640) / NT > 0 ? (stage == 1 ? 768 : 640) / NT : 1) : 1;
+        return sizeof(R) == 4 ? ((stage == 1 ? 640 : 512) / NT > 0 ? (stage == 1 ? 640 : 512) / NT : 1) : 1;
     }
 };
 
@@ -216,30 +217,341 @@ __device__ __forceinline__ void block_reduce_store(T (&v)[NV], const bool* is_ma
     }
 }
 
-// x-reconstruction of one cell in shared memory (two records at xr[t] and xr[NT + t]);
-// the float32 form's cell depth and bed come from the cell record (h0, z).
+// One side of a reconstructed cell as a face sees it: depth, normal and tangential
+// velocity, and X = the recovered bed (float64) or the in-cell bed slope d (float32),
+// S = the in-cell surface slope sE (float32).  The cell's own bed z and depth h0 (the
+// float32 flux's difference form) come with the cell record.
 template <class R>
-__device__ __forceinline__ void store_recon(Q4<R>* xr, int t, int nt, const Recon<R>& r) {
-    xr[t] = Q4<R>{r.Hm, r.Hp, r.Um, r.Up};
-    if constexpr (sizeof(R) == 8) xr[nt + t] = Q4<R>{r.Vm, r.Vp, r.Zm, r.Zp};
-    else xr[nt + t] = Q4<R>{r.Vm, r.Vp, r.d, r.sE};
+struct Side {
+    R H, U, V, X, S;
+};
+template <class R>
+__device__ __forceinline__ Side<R> side_plus(const Recon<R>& r) {
+    if constexpr (sizeof(R) == 8) return Side<R>{r.Hp, r.Up, r.Vp, r.Zp, R(0)};
+    else return Side<R>{r.Hp, r.Up, r.Vp, r.d, r.sE};
+}
+template <class R>
+__device__ __forceinline__ Side<R> side_minus(const Recon<R>& r) {
+    if constexpr (sizeof(R) == 8) return Side<R>{r.Hm, r.Um, r.Vm, r.Zm, R(0)};
+    else return Side<R>{r.Hm, r.Um, r.Vm, r.d, r.sE};
 }
 
+// Face flux from the plus side of the cell below / west of the face (bed zl, depth hl)
+// and the minus side of the cell above / east of it: face_flux's arithmetic exactly.
 template <class R>
-__device__ __forceinline__ Recon<R> load_recon(const Q4<R>* xr, int t, int nt, R h0, R z) {
-    const Q4<R> p = xr[t], q = xr[nt + t];
-    Recon<R> r;
-    r.Hm = p.a; r.Hp = p.b; r.Um = p.c; r.Up = p.d;
-    r.Vm = q.a; r.Vp = q.b;
+__device__ __forceinline__ Q4<R> side_flux(const KC<R>& c, const Side<R>& L, R zl, R hl, const Side<R>& Rt, R zr,
+                                           R hr) {
+    Recon<R> a, b;
+    a.Hp = L.H; a.Up = L.U; a.Vp = L.V;
+    b.Hm = Rt.H; b.Um = Rt.U; b.Vm = Rt.V;
     if constexpr (sizeof(R) == 8) {
-        r.Zm = q.c; r.Zp = q.d;
-        r.z = r.d = r.h0 = r.sE = R(0);
+        a.Zp = L.X; b.Zm = Rt.X;
     } else {
-        r.d = q.c; r.sE = q.d;
-        r.z = z; r.h0 = h0;
-        r.Zm = r.Zp = R(0);
+        a.d = L.X; a.sE = L.S; a.z = zl; a.h0 = hl;
+        b.d = Rt.X; b.sE = Rt.S; b.z = zr; b.h0 = hr;
     }
-    return r;
+    (void)zl; (void)hl; (void)zr; (void)hr;
+    Q4<R> f;
+    face_flux(c, a, b, f.a, f.b, f.c, f.d);
+    return f;
+}
+
+// The row-marching pipeline of one strip chunk (see the head of this file).  Row r is
+// the newest row built; per row two barriers separate the phases:
+//   A  build row r into the ring, prefetch row r+2 and the update inputs of row r-3;
+//      y-reconstruction of row r-1 and the y-face between rows r-2 and r-1 (own
+//      column, registers); x-reconstruction of row r-2 (neighbours from the ring),
+//      its plus side published for the next thread
+//   -- barrier --
+//   B  x-face between columns cx-1 and cx of row r-2, published for thread t-1
+//   -- barrier --
+//   C  theta of row r-2, published for the neighbours
+//   D  update of row r-3: its own fluxes and thetas from registers, the east face and
+//      the west / east thetas from the previous row's shared entries
+// row<true> is the steady state: every row touched lies inside the grid, so the
+// range tests, y-ghosts and domain-edge terms drop out; row<false> handles the
+// pipeline fill at the chunk's start, the drain at its end and the grid's edges.
+template <class R, int NT, int STAGE>
+struct StripPipe {
+    using G = StripGeom<R, NT>;
+    static constexpr int P = G::P;
+    Q4<R>* s_cell;
+    Q4<R>* s_rp;
+    Q4<R>* s_xf;
+    R* s_rs;
+    R* s_th;
+    const Grid<R>& gd;
+    const KC<R>& c;
+    const R* bcv;
+    float* const* s_snap;
+    const R* __restrict__ H;
+    const R* __restrict__ HU;
+    const R* __restrict__ HV;
+    int t, ts, cx, cxc, nx, ny, y0, y1, scol, xside, xkind;
+    bool col_in, do_out, west, east;
+    R dt, rdx, rdy, idx, idy, rdt, tt;
+    // carried state of this thread's column
+    HaloRaw<R> ra, rb;                 // raw rows r+1 and r+2 (prefetched)
+    Q4<R> c1, c2;                      // cells of rows r-1 and r-2 {h, u, v, z}
+    R h3;                              // depth of row r-3
+    Side<R> ylow;                      // plus side of the y-reconstruction of row r-2
+    Q4<R> yf1, yf2;                    // y-faces r-2 and r-3
+    Q4<R> xf1;                         // own x-face of row r-3
+    R th1, th2;                        // theta of rows r-3 and r-4
+    R by1, by2, bx1;                   // bed terms: y of rows r-2, r-3; x of row r-3
+    CellIn<R> cin;
+    R acc_clip, xin, xout, yin, yout, infil, rainw, rate, hsum, ssum, hmax;
+
+    // Raw values of an interior row at this thread's source column (its own column, or
+    // the layer an x-ghost copies)
+    __device__ __forceinline__ HaloRaw<R> fetch_in(int gy) const {
+        const size_t i = (size_t)gy * nx + scol;
+        return HaloRaw<R>{H[i], HU[i], HV[i], gd.z[i]};
+    }
+    // halo_build for a row inside the grid: an interior cell, or the x-ghost that the
+    // x-sweep would see (boundaries.py:81-128)
+    __device__ __forceinline__ Q4<R> build_in(const HaloRaw<R>& a) const {
+        R u0, v0;
+        kp_velocity(c, a.h, a.hu, a.hv, u0, v0);
+        if (xkind < 0) return Q4<R>{a.h, u0, v0, a.z};
+        const R sgn = xside == EDGE_W ? R(-1) : R(1);
+        const R un = sgn * u0, ut = v0;
+        R hg, ung, utg;
+        if (xkind == BC_CLOSED) { hg = a.h; ung = -un; utg = ut; }
+        else if (xkind == BC_TRANSMISSIVE) { hg = a.h; ung = un; utg = ut; }
+        else if (xkind == BC_STAGE) stage_ghost(c, bcv[xside], a.h, un, ut, a.z, hg, ung, utg);
+        else discharge_ghost(c, bcv[xside], a.h, hg, ung, utg);
+        return Q4<R>{hg, sgn * ung, utg, a.z};
+    }
+
+    template <bool FULL>
+    __device__ __forceinline__ void row(const int r) {
+        const int s0 = (r & (G::RING - 1)) * P, s2 = ((r - 2) & (G::RING - 1)) * P;
+        const int xo = ((r - 2) & 1) * P, xp = ((r - 3) & 1) * P;
+        const int orow = r - 3, row = r - 2;
+        const bool upd = FULL || (orow >= y0 && orow < y1);
+        // ---- A: row r, prefetches, y-face r-1, x-reconstruction of row r-2
+        Q4<R> c0;
+        if (FULL) {
+            c0 = build_in(ra);
+        } else {
+            halo_build(c, gd, bcv, ra, cx, r, c0.a, c0.b, c0.c, c0.d);
+        }
+        s_cell[s0 + ts] = c0;
+        ra = rb;
+        rb = FULL ? fetch_in(r + 2) : halo_fetch(c, gd, H, HU, HV, cx, r + 2);
+        if (upd) cin = cell_fetch<R, STAGE>(gd, (size_t)orow * nx + cxc);
+        Q4<R> yf0{R(0), R(0), R(0), R(0)};
+        R by0 = R(0), bx0 = R(0);
+        if (FULL || r >= y0 - 1) {
+            // y-reconstruction of row r-1: normal velocity v, tangential u
+            const Recon<R> yup = reconstruct(c, c2.a, c1.a, c0.a, c2.c, c1.c, c0.c, c2.b, c1.b, c0.b, c2.d, c1.d, c0.d);
+            const int fy = r - 1;
+            if (FULL || (r >= y0 && fy >= 0 && fy <= ny)) yf0 = side_flux(c, ylow, c2.d, c2.a, side_minus(yup), c1.d, c1.a);
+            ylow = side_plus(yup);
+            if (c.order == 2) by0 = bed_term(c, yup);
+        }
+        const bool xact = FULL || (r >= y0 + 1 && (unsigned)row < (unsigned)ny);
+        Q4<R> cl;
+        Side<R> xm;
+        if (xact) {
+            cl = s_cell[s2 + ts - 1];
+            const Q4<R> cr = s_cell[s2 + ts + 1];
+            const Recon<R> xr = reconstruct(c, cl.a, c2.a, cr.a, cl.b, c2.b, cr.b, cl.c, c2.c, cr.c, cl.d, c2.d, cr.d);
+            const Side<R> xp_ = side_plus(xr);
+            s_rp[ts] = Q4<R>{xp_.H, xp_.U, xp_.V, xp_.X};
+            if constexpr (sizeof(R) == 4) s_rs[ts] = xp_.S;
+            xm = side_minus(xr);
+            if (c.order == 2) bx0 = bed_term(c, xr);
+        }
+        __syncthreads();
+        // ---- B: x-face between columns cx-1 and cx of row r-2
+        Q4<R> xf0{R(0), R(0), R(0), R(0)};
+        if (xact) {
+            const Q4<R> lp = s_rp[ts - 1];
+            Side<R> L{lp.a, lp.b, lp.c, lp.d, R(0)};
+            if constexpr (sizeof(R) == 4) L.S = s_rs[ts - 1];
+            xf0 = side_flux(c, L, cl.d, cl.a, xm, c2.d, c2.a);
+            s_xf[xo + ts] = xf0;
+        }
+        __syncthreads();
+        // ---- C: theta of row r-2 (swe2d.py:259-264); 1 outside the grid
+        R th0 = R(1);
+        if (FULL || r >= y0 + 1) {
+            if (FULL || (unsigned)row < (unsigned)ny) {
+                const R Fw = xf0.a, Fe = s_xf[xo + ts + 1].a, Gs = yf1.a, Gn = yf0.a;
+                const R out = per_len(relu(Fe) + relu(-Fw), rdx, idx) + per_len(relu(Gn) + relu(-Gs), rdy, idy);
+                const R need = out * dt;
+                const R hh = c2.a;
+                const R th = need > hh ? hh / (need > R(0) ? need : R(1)) : R(1);
+                th0 = col_in ? th : R(1);
+            }
+            s_th[xo + ts] = th0;
+        }
+        // ---- D: update of row r-3
+        if (upd) update<FULL>(orow, xp, th0);
+        // ---- shift the carried column
+        h3 = c2.a;
+        c2 = c1;
+        c1 = c0;
+        yf2 = yf1;
+        yf1 = yf0;
+        by2 = by1;
+        by1 = by0;
+        bx1 = bx0;
+        xf1 = xf0;
+        th2 = th1;
+        th1 = th0;
+    }
+
+    template <bool FULL>
+    __device__ __forceinline__ void update(const int orow, const int xp, const R thN) {
+        const R thC = th1, thS = th2;
+        const R thW = s_th[xp + ts - 1], thE = s_th[xp + ts + 1];
+        const Q4<R> xw = xf1, xe = s_xf[xp + ts + 1], ys = yf2, yn = yf1;
+        const R Fw = xw.a, Fe = xe.a, Gs = ys.a, Gn = yn.a;
+        const R sw = Fw > R(0) ? thW : thC, se = Fe > R(0) ? thC : thE;
+        const R ss = Gs > R(0) ? thS : thC, sn = Gn > R(0) ? thC : thN;
+        const R F1w = Fw * sw, F1e = Fe * se, G1s = Gs * ss, G1n = Gn * sn;
+        R a1 = per_len(-(F1e - F1w), rdx, idx);
+        R a2 = per_len(-(xe.b - xw.c), rdx, idx);
+        R a3 = per_len(-(xe.d * se - xw.d * sw), rdx, idx);
+        R b1 = per_len(-(G1n - G1s), rdy, idy);
+        R b2 = per_len(-(yn.b - ys.c), rdy, idy);
+        R b3 = per_len(-(yn.d * sn - ys.d * ss), rdy, idy);
+        if (c.order == 2) {
+            a2 = a2 + per_len(bx1, rdx, idx);
+            b2 = b2 + per_len(by2, rdy, idy);
+        }
+        const R dh = a1 + b1, dhu = a2 + b3, dhv = a3 + b2;
+        if (!do_out) return;
+        if (west) { xin += relu(F1w); xout += relu(-F1w); }
+        if (east) { xin += relu(-F1e); xout += relu(F1e); }
+        if (!FULL) {
+            if (orow == 0) { yin += relu(G1s); yout += relu(-G1s); }
+            if (orow == ny - 1) { yin += relu(-G1n); yout += relu(G1n); }
+        }
+        const size_t i = (size_t)orow * nx + cx;
+        R hn, hun, hvn;
+        if (STAGE == 2) {
+            hn = R(0.5) * (cin.h0 + h3 + dt * dh);
+            hun = R(0.5) * (cin.hu0 + cin.hu1 + dt * dhu);
+            hvn = R(0.5) * (cin.hv0 + cin.hv1 + dt * dhv);
+        } else {
+            hn = h3 + dt * dh;
+            hun = cin.hu0 + dt * dhu;
+            hvn = cin.hv0 + dt * dhv;
+        }
+        const R neg = clamp0(-hn);
+        acc_clip += neg;
+        hn = hn + neg;
+        if (STAGE == 1) {
+            gd.h1[i] = hn; gd.hu1[i] = hun; gd.hv1[i] = hvn;
+            return;
+        }
+        // ---- rain, Horton infiltration, retention store (swe2d.py:330-360)
+        R sf = cin.sf;
+        if (gd.rw) {
+            const R add = rdt * cin.rw;
+            hn = hn + add;
+            rainw += add;
+        } else {
+            hn = hn + rdt;
+        }
+        if (gd.f0) {
+            const R rate_f = cin.fc + (cin.f0 - cin.fc) * rexp(-cin.k * tt);
+            const R pot = rate_f * dt;
+            const R take = rmin(pot, hn);
+            const R safe = hn > R(0) ? hn : R(1);
+            const R scale = hn > R(0) ? (hn - take) / safe : R(0);
+            hn = hn - take;
+            hun = hun * scale;
+            hvn = hvn * scale;
+            R taken = take;
+            if (gd.S) {
+                const R tks = rmin(pot - take, sf);
+                sf = sf - tks;
+                taken = taken + tks;
+            }
+            infil += taken;
+            gd.ic[i] = cin.ic + taken;
+        }
+        if (gd.S) {
+            const R room = clamp0(cin.S - sf);
+            const R fill = rmin(room, hn);
+            const R safe = hn > R(0) ? hn : R(1);
+            const R scale = hn > R(0) ? (hn - fill) / safe : R(0);
+            hn = hn - fill;
+            hun = hun * scale;
+            hvn = hvn * scale;
+            sf = sf + fill;
+            gd.sf[i] = sf;
+        }
+        // ---- semi-implicit Manning friction (swe2d.py:362-370)
+        R u, v, ks = R(0);
+        if constexpr (sizeof(R) == 4) {
+            // KP factor of the new depth, kept for the CFL velocity below
+            const float h2 = hn * hn, h4 = h2 * h2;
+            ks = hn >= c.h_dry ? 1.4142135623730951f * hn * rsqrtf(h4 + fmaxf(h4, c.kp_eps)) : 0.0f;
+            u = hun * ks;
+            v = hvn * ks;
+        } else {
+            kp_velocity(c, hn, hun, hvn, u, v);
+        }
+        const R speed = dsqrt(u * u + v * v);
+        const R hf = rmax(hn, c.h_dry);
+        const R nm = cin.n;
+        const R denom = R(1) + dt * c.g * nm * nm * speed / pow43(hf);
+        u = u / denom;
+        v = v / denom;
+        const bool wet = hn >= c.h_dry;
+        hun = wet ? hn * u : R(0);
+        hvn = wet ? hn * v : R(0);
+        if (STAGE == 2) {
+            gd.h[i] = hn; gd.hu[i] = hun; gd.hv[i] = hvn;
+        } else {
+            gd.h1[i] = hn; gd.hu1[i] = hun; gd.hv1[i] = hvn;
+        }
+        if (gd.pk) gd.pk[i] = rmax(gd.pk[i], hn);
+        // ---- CFL rate of the new state for the next step (swe2d.py:179-184)
+        R u2, v2;
+        if constexpr (sizeof(R) == 4) {
+            u2 = hun * ks;
+            v2 = hvn * ks;
+        } else {
+            kp_velocity(c, hn, hun, hvn, u2, v2);
+        }
+        // running peak speed and output use the KP velocities of the new state, as the
+        // reference's snapshots do (swe2d.py:161-167, coupling.py:229-242)
+        if (gd.ps) gd.ps[i] = rmax(gd.ps[i], dsqrt(u2 * u2 + v2 * v2));
+        if (float* sh = s_snap[0]) {
+            sh[i] = (float)hn;
+            s_snap[1][i] = (float)u2;
+            s_snap[2][i] = (float)v2;
+        }
+        const R cw = dsqrt(c.g * hn);
+        const R rr = hn > c.h_dry ? per_len(fabs(u2) + cw, rdx, idx) + per_len(fabs(v2) + cw, rdy, idy) : R(0);
+        rate = rmax(rate, rr);
+        hsum += hn;
+        ssum += sf;
+        hmax = rmax(hmax, hn);
+    }
+};
+
+// Source column of an x-ghost: the layer of the grid it copies (boundaries.py:104-116),
+// as halo_fetch picks it; the column itself inside the grid.
+template <class R>
+__device__ __forceinline__ int ghost_source_column(const KC<R>& c, const Grid<R>& gd, int cx) {
+    const int nx = gd.nx;
+    if ((unsigned)cx < (unsigned)nx) return cx;
+    const int ng = c.order == 1 ? 1 : 2;
+    const bool lo = cx < 0;
+    const int k = lo ? (-cx - 1) : (cx - nx);
+    const int kind = gd.bc[lo ? EDGE_W : EDGE_E];
+    int layer;
+    if (kind == BC_CLOSED || kind == BC_TRANSMISSIVE) layer = nx < ng ? (lo ? 0 : nx - 1) : (lo ? k : nx - 1 - k);
+    else layer = lo ? 0 : nx - 1;
+    return layer < 0 ? 0 : (layer > nx - 1 ? nx - 1 : layer);
 }
 
 // STAGE: 0 = first-order full step, 1 = RK stage 1, 2 = RK stage 2 + sources.
@@ -253,13 +565,8 @@ __global__ void __launch_bounds__(NT, StripGeom<R, NT>::min_ctas(STAGE)) strip_k
                                                     const StepParams* __restrict__ params, const KC<R> c,
                                                     double* __restrict__ partials) {
     using G = StripGeom<R, NT>;
+    constexpr int P = G::P;
     extern __shared__ __align__(32) unsigned char smem_raw[];
-    Q4<R>* s_cell = reinterpret_cast<Q4<R>*>(smem_raw);   // [RING][NT] {h, u, v, z}
-    Q4<R>* s_xr = s_cell + G::RING * NT;                  // [2][NT] x-reconstruction
-    Q4<R>* s_xf = s_xr + 2 * NT;                          // [FRX][NT] x-faces {F1, F2L, F2R, F3}
-    Q4<R>* s_yf = s_xf + G::FRX * NT;                     // [FR][NT] y-faces
-    R* s_th = reinterpret_cast<R*>(s_yf + G::FR * NT);    // [FR][NT] theta
-    R* red = reinterpret_cast<R*>(smem_raw);              // after the row loop
     __shared__ R bcv[4];
     __shared__ float* s_snap[3];                      // output slots of this step (stage 0 / 2)
     // the member's record, staged once: its field pointers are re-read every row, and
@@ -276,267 +583,73 @@ __global__ void __launch_bounds__(NT, StripGeom<R, NT>::min_ctas(STAGE)) strip_k
         unsigned* dst = reinterpret_cast<unsigned*>(&s_gd);
         for (int k = t; k < (int)(sizeof(Grid<R>) / 4); k += NT) dst[k] = src[k];
     }
-    __syncthreads();
-    const Grid<R>& gd = s_gd;
-    const int nx = gd.nx, ny = gd.ny;
-    const int x0 = sr.x0, W = sr.w, y0 = sr.y0, y1 = sr.y1;
-    const int cx = x0 - 3 + t;                        // this thread's column
-    const R dt = par_dt<R>(pr);
     if (t < 4) bcv[t] = par_bc<R>(pr, STAGE == 2, t);
     if (t == 0) {
         s_snap[0] = STAGE != 1 ? pr.snap_h : nullptr;
         s_snap[1] = pr.snap_u;
         s_snap[2] = pr.snap_v;
     }
-    const R* __restrict__ H = STAGE == 2 ? gd.h1 : gd.h;
-    const R* __restrict__ HU = STAGE == 2 ? gd.hu1 : gd.hu;
-    const R* __restrict__ HV = STAGE == 2 ? gd.hv1 : gd.hv;
-    const R rdx = gd.rdx, rdy = gd.rdy, idx = gd.idx, idy = gd.idy;
-    const R rdt = par_rain<R>(pr) * dt;
-    const R tt = clamp0(par_t<R>(pr) - gd.rt0);
-    const bool col_in = (unsigned)cx < (unsigned)nx;
-    const int q = cx - x0;                                      // column relative to the strip
-    const bool do_yface = q >= -1 && q <= W && col_in;
-    const bool do_xrec = q >= -2 && q <= W + 1;
-    const bool do_xface = q >= -1 && q <= W + 1 && cx >= 0 && cx <= nx;
-    const bool do_theta = q >= -1 && q <= W;                    // theta = 1 outside the domain
-    const bool do_out = q >= 0 && q < W && col_in;
-
-    R acc_clip = 0, xin = 0, xout = 0, yin = 0, yout = 0, infil = 0, rainw = 0, rate = 0, hsum = 0, ssum = 0;
-    R hmax = 0;
-    Recon<R> ylow;                                   // y-reconstruction of row r-2 (carried)
-    R by1 = R(0), by2 = R(0);                        // y bed terms of rows r-2 and r-3
-    R bxc = R(0);                                    // x bed term of row r-3
-    R h_r3 = R(0);                                   // depth of this column in row r-3
-    // software pipeline: halo rows are fetched two rows ahead, update inputs at the start
-    // of the iteration that uses them
-    HaloRaw<R> ra = halo_fetch(c, gd, H, HU, HV, cx, y0 - 3);
-    HaloRaw<R> rb = halo_fetch(c, gd, H, HU, HV, cx, y0 - 2);
-    CellIn<R> cin;
+    __syncthreads();
+    const Grid<R>& gd = s_gd;
+    Q4<R>* s_cell = reinterpret_cast<Q4<R>*>(smem_raw);
+    StripPipe<R, NT, STAGE> pp{s_cell, s_cell + G::RING * P, s_cell + (G::RING + 1) * P,
+                               reinterpret_cast<R*>(s_cell + (G::RING + 3) * P),
+                               reinterpret_cast<R*>(s_cell + (G::RING + 3) * P) + P, gd, c, bcv, s_snap,
+                               STAGE == 2 ? gd.h1 : gd.h, STAGE == 2 ? gd.hu1 : gd.hu, STAGE == 2 ? gd.hv1 : gd.hv};
+    const int nx = gd.nx, ny = gd.ny;
+    const int x0 = sr.x0, W = sr.w, y0 = sr.y0, y1 = sr.y1;
+    const int cx = x0 - 3 + t;                        // this thread's column
+    const int q = cx - x0;                            // column relative to the strip
+    pp.t = t;
+    pp.ts = t + 1;
+    pp.cx = cx;
+    pp.cxc = cx < 0 ? 0 : (cx > nx - 1 ? nx - 1 : cx);
+    pp.nx = nx;
+    pp.ny = ny;
+    pp.y0 = y0;
+    pp.y1 = y1;
+    pp.col_in = (unsigned)cx < (unsigned)nx;
+    pp.do_out = q >= 0 && q < W && pp.col_in;
+    pp.west = cx == 0;
+    pp.east = cx == nx - 1;
+    pp.scol = ghost_source_column(c, gd, cx);
+    pp.xside = cx < 0 ? EDGE_W : EDGE_E;
+    pp.xkind = pp.col_in ? -1 : gd.bc[pp.xside];
+    pp.dt = par_dt<R>(pr);
+    pp.rdx = gd.rdx;
+    pp.rdy = gd.rdy;
+    pp.idx = gd.idx;
+    pp.idy = gd.idy;
+    pp.rdt = par_rain<R>(pr) * pp.dt;
+    pp.tt = clamp0(par_t<R>(pr) - gd.rt0);
+    pp.acc_clip = pp.xin = pp.xout = pp.yin = pp.yout = pp.infil = pp.rainw = pp.rate = pp.hsum = pp.ssum = R(0);
+    pp.hmax = R(0);
+    pp.by1 = pp.by2 = pp.bx1 = R(0);
+    pp.th1 = pp.th2 = R(1);
+    pp.h3 = R(0);
+    // software pipeline: raw rows are fetched two rows ahead
+    pp.ra = halo_fetch(c, gd, pp.H, pp.HU, pp.HV, cx, y0 - 3);
+    pp.rb = halo_fetch(c, gd, pp.H, pp.HU, pp.HV, cx, y0 - 2);
     static_assert((G::RING & (G::RING - 1)) == 0, "ring slots are row & (RING - 1)");
+    // steady-state rows: every row touched (r-4 .. r+2) inside the grid, the update row
+    // neither the first nor the last row of the grid
+    const int r_lo = max(y0 + 3, 4), r_hi = min(y1 + 2, ny - 3);
+    int r = y0 - 3;
+    for (; r <= y1 + 2 && r < r_lo; ++r) pp.template row<false>(r);
+    for (; r <= r_hi; ++r) pp.template row<true>(r);
+    for (; r <= y1 + 2; ++r) pp.template row<false>(r);
     __syncthreads();
-
-    for (int r = y0 - 3; r <= y1 + 2; ++r) {
-        const int s0 = r & (G::RING - 1), s1 = (r - 1) & (G::RING - 1);   // ring slots of rows r, r-1,
-        const int s2 = (r - 2) & (G::RING - 1), s3 = (r - 3) & (G::RING - 1);  // r-2 and r-3
-        // ---- P1: build row r from values fetched two rows ago; fetch row r + 2 and the
-        //      update inputs of row r - 2
-        const int sl = s0;
-        const HaloRaw<R> rnext = halo_fetch(c, gd, H, HU, HV, cx, r + 2);
-        // update inputs of row r-3, consumed after three barriers of this iteration
-        if (do_out && r - 3 >= y0 && r - 3 < y1) cin = cell_fetch<R, STAGE>(gd, (size_t)(r - 3) * nx + cx);
-        {
-            R hh, uu, vv, zz;
-            halo_build(c, gd, bcv, ra, cx, r, hh, uu, vv, zz);
-            s_cell[sl * NT + t] = Q4<R>{hh, uu, vv, zz};
-        }
-        ra = rb;
-        rb = rnext;
-        __syncthreads();
-        // ---- P2: y-face between rows r-2 and r-1 (face index r-1), x-reconstruction of row r-2
-        R by_new = R(0), bx_new = R(0);
-        Q4<R> cm2{};                                 // cell (row r-2, this column)
-        if (r >= y0 - 1) {
-            cm2 = s_cell[s2 * NT + t];
-            if (do_yface) {
-                // y-reconstruction of row r-1: normal v, tangential u
-                const Q4<R> cb = s_cell[s1 * NT + t], cc = s_cell[s0 * NT + t];
-                Recon<R> yup = reconstruct(c, cm2.a, cb.a, cc.a, cm2.c, cb.c, cc.c, cm2.b, cb.b, cc.b,
-                                           cm2.d, cb.d, cc.d);
-                const int fy = r - 1;
-                if (r >= y0 && fy >= y0 - 1 && fy <= y1 + 1) {
-                    R F1 = R(0), F2L = R(0), F2R = R(0), F3 = R(0);
-                    if (fy >= 0 && fy <= ny) face_flux(c, ylow, yup, F1, F2L, F2R, F3);
-                    s_yf[(fy & (G::FR - 1)) * NT + t] = Q4<R>{F1, F2L, F2R, F3};
-                }
-                ylow = yup;
-                if (c.order == 2) by_new = bed_term(c, yup);
-            }
-            if (r >= y0 + 1 && do_xrec) {
-                const Q4<R> cl = s_cell[s2 * NT + t - 1], cr = s_cell[s2 * NT + t + 1];
-                Recon<R> xr = reconstruct(c, cl.a, cm2.a, cr.a, cl.b, cm2.b, cr.b, cl.c, cm2.c, cr.c,
-                                          cl.d, cm2.d, cr.d);
-                store_recon(s_xr, t, NT, xr);
-                if (c.order == 2) bx_new = bed_term(c, xr);
-            }
-        }
-        __syncthreads();
-        if (r >= y0 + 1) {
-            const int row = r - 2;
-            // ---- P3: x-faces of row r-2 (face cx between columns cx-1 and cx)
-            if (do_xface && (unsigned)row < (unsigned)ny) {
-                const Q4<R> cl = s_cell[s2 * NT + t - 1];
-                Recon<R> L = load_recon(s_xr, t - 1, NT, cl.a, cl.d), Rr = load_recon(s_xr, t, NT, cm2.a, cm2.d);
-                R F1, F2L, F2R, F3;
-                face_flux(c, L, Rr, F1, F2L, F2R, F3);
-                s_xf[(row & (G::FRX - 1)) * NT + t] = Q4<R>{F1, F2L, F2R, F3};
-            }
-            __syncthreads();
-            // ---- P4: theta of row r-2
-            if (do_theta) {
-                R th = R(1);
-                if ((unsigned)row < (unsigned)ny && col_in) {
-                    const int fr = (row & (G::FR - 1)) * NT, frx = (row & (G::FRX - 1)) * NT;
-                    const R Fw = s_xf[frx + t].a, Fe = s_xf[frx + t + 1].a;
-                    const R Gs = s_yf[fr + t].a, Gn = s_yf[((row + 1) & (G::FR - 1)) * NT + t].a;
-                    const R out = per_len(relu(Fe) + relu(-Fw), rdx, idx) + per_len(relu(Gn) + relu(-Gs), rdy, idy);
-                    const R need = out * dt;
-                    const R hh = cm2.a;
-                    th = need > hh ? hh / (need > R(0) ? need : R(1)) : R(1);
-                }
-                s_th[(row & (G::FR - 1)) * NT + t] = th;
-            }
-            __syncthreads();
-        }
-        // ---- P5: update row r-3
-        const int orow = r - 3;
-        if (orow >= y0 && orow < y1 && do_out) {
-            const int f0 = (orow & (G::FR - 1)) * NT, f1 = ((orow + 1) & (G::FR - 1)) * NT;
-            const int fx = (orow & (G::FRX - 1)) * NT;
-            const int tc = f0 + t;
-            const R thC = s_th[tc], thW = s_th[tc - 1], thE = s_th[tc + 1];
-            const R thS = s_th[((orow - 1) & (G::FR - 1)) * NT + t], thN = s_th[f1 + t];
-            const Q4<R> xw = s_xf[fx + t], xe = s_xf[fx + t + 1], ys = s_yf[f0 + t], yn = s_yf[f1 + t];
-            const R Fw = xw.a, Fe = xe.a, Gs = ys.a, Gn = yn.a;
-            const R sw = Fw > R(0) ? thW : thC, se = Fe > R(0) ? thC : thE;
-            const R ss = Gs > R(0) ? thS : thC, sn = Gn > R(0) ? thC : thN;
-            const R F1w = Fw * sw, F1e = Fe * se, G1s = Gs * ss, G1n = Gn * sn;
-            R a1 = per_len(-(F1e - F1w), rdx, idx);
-            R a2 = per_len(-(xe.b - xw.c), rdx, idx);
-            R a3 = per_len(-(xe.d * se - xw.d * sw), rdx, idx);
-            R b1 = per_len(-(G1n - G1s), rdy, idy);
-            R b2 = per_len(-(yn.b - ys.c), rdy, idy);
-            R b3 = per_len(-(yn.d * sn - ys.d * ss), rdy, idy);
-            if (c.order == 2) {
-                a2 = a2 + per_len(bxc, rdx, idx);
-                b2 = b2 + per_len(by2, rdy, idy);
-            }
-            const R dh = a1 + b1, dhu = a2 + b3, dhv = a3 + b2;
-            if (cx == 0) { xin += relu(F1w); xout += relu(-F1w); }
-            if (cx == nx - 1) { xin += relu(-F1e); xout += relu(F1e); }
-            if (orow == 0) { yin += relu(G1s); yout += relu(-G1s); }
-            if (orow == ny - 1) { yin += relu(-G1n); yout += relu(G1n); }
-            const size_t i = (size_t)orow * nx + cx;
-            R hn, hun, hvn;
-            if (STAGE == 2) {
-                const R h1 = h_r3;
-                hn = R(0.5) * (cin.h0 + h1 + dt * dh);
-                hun = R(0.5) * (cin.hu0 + cin.hu1 + dt * dhu);
-                hvn = R(0.5) * (cin.hv0 + cin.hv1 + dt * dhv);
-            } else {
-                hn = h_r3 + dt * dh;
-                hun = cin.hu0 + dt * dhu;
-                hvn = cin.hv0 + dt * dhv;
-            }
-            const R neg = clamp0(-hn);
-            acc_clip += neg;
-            hn = hn + neg;
-            if (STAGE == 1) {
-                gd.h1[i] = hn; gd.hu1[i] = hun; gd.hv1[i] = hvn;
-            } else {
-                // ---- rain, Horton infiltration, retention store (swe2d.py:330-360)
-                R sf = cin.sf;
-                if (gd.rw) {
-                    const R add = rdt * cin.rw;
-                    hn = hn + add;
-                    rainw += add;
-                } else {
-                    hn = hn + rdt;
-                }
-                if (gd.f0) {
-                    const R rate_f = cin.fc + (cin.f0 - cin.fc) * rexp(-cin.k * tt);
-                    const R pot = rate_f * dt;
-                    const R take = rmin(pot, hn);
-                    const R safe = hn > R(0) ? hn : R(1);
-                    const R scale = hn > R(0) ? (hn - take) / safe : R(0);
-                    hn = hn - take;
-                    hun = hun * scale;
-                    hvn = hvn * scale;
-                    R taken = take;
-                    if (gd.S) {
-                        const R tks = rmin(pot - take, sf);
-                        sf = sf - tks;
-                        taken = taken + tks;
-                    }
-                    infil += taken;
-                    gd.ic[i] = cin.ic + taken;
-                }
-                if (gd.S) {
-                    const R room = clamp0(cin.S - sf);
-                    const R fill = rmin(room, hn);
-                    const R safe = hn > R(0) ? hn : R(1);
-                    const R scale = hn > R(0) ? (hn - fill) / safe : R(0);
-                    hn = hn - fill;
-                    hun = hun * scale;
-                    hvn = hvn * scale;
-                    sf = sf + fill;
-                    gd.sf[i] = sf;
-                }
-                // ---- semi-implicit Manning friction (swe2d.py:362-370)
-                R u, v, ks = R(0);
-                if constexpr (sizeof(R) == 4) {
-                    // KP factor of the new depth, kept for the CFL velocity below
-                    const float h2 = hn * hn, h4 = h2 * h2;
-                    ks = hn >= c.h_dry ? 1.4142135623730951f * hn * rsqrtf(h4 + fmaxf(h4, c.kp_eps)) : 0.0f;
-                    u = hun * ks;
-                    v = hvn * ks;
-                } else {
-                    kp_velocity(c, hn, hun, hvn, u, v);
-                }
-                const R speed = dsqrt(u * u + v * v);
-                const R hf = rmax(hn, c.h_dry);
-                const R nm = cin.n;
-                const R denom = R(1) + dt * c.g * nm * nm * speed / pow43(hf);
-                u = u / denom;
-                v = v / denom;
-                const bool wet = hn >= c.h_dry;
-                hun = wet ? hn * u : R(0);
-                hvn = wet ? hn * v : R(0);
-                if (STAGE == 2) {
-                    gd.h[i] = hn; gd.hu[i] = hun; gd.hv[i] = hvn;
-                } else {
-                    gd.h1[i] = hn; gd.hu1[i] = hun; gd.hv1[i] = hvn;
-                }
-                if (gd.pk) gd.pk[i] = rmax(gd.pk[i], hn);
-                // ---- CFL rate of the new state for the next step (swe2d.py:179-184)
-                R u2, v2;
-                if constexpr (sizeof(R) == 4) {
-                    u2 = hun * ks;
-                    v2 = hvn * ks;
-                } else {
-                    kp_velocity(c, hn, hun, hvn, u2, v2);
-                }
-                // running peak speed and output use the KP velocities of the new state, as the
-                // reference's snapshots do (swe2d.py:161-167, coupling.py:229-242)
-                if (gd.ps) gd.ps[i] = rmax(gd.ps[i], dsqrt(u2 * u2 + v2 * v2));
-                if (float* sh = s_snap[0]) {
-                    sh[i] = (float)hn;
-                    s_snap[1][i] = (float)u2;
-                    s_snap[2][i] = (float)v2;
-                }
-                const R cw = dsqrt(c.g * hn);
-                const R rr = hn > c.h_dry ? per_len(fabs(u2) + cw, rdx, idx) + per_len(fabs(v2) + cw, rdy, idy) : R(0);
-                rate = rmax(rate, rr);
-                hsum += hn;
-                ssum += sf;
-                hmax = rmax(hmax, hn);
-            }
-        }
-        by2 = by1;
-        by1 = by_new;
-        bxc = bx_new;
-        h_r3 = cm2.a;
-    }
-    __syncthreads();
+    R* red = reinterpret_cast<R*>(smem_raw);
     double* out = partials + (size_t)blockIdx.x * NPART;
     if (STAGE == 1) {
-        R v[5] = {acc_clip, xin, xout, yin, yout};
+        R v[5] = {pp.acc_clip, pp.xin, pp.xout, pp.yin, pp.yout};
         const bool mx[5] = {false, false, false, false, false};
         const int sl[5] = {P_CLIP1, P_XIN1, P_XOUT1, P_YIN1, P_YOUT1};
         block_reduce_store<5>(v, mx, red, out, sl, NT);
     } else {
         const int b = STAGE == 2 ? P_CLIP2 : P_CLIP1;
-        R v[11] = {acc_clip, xin, xout, yin, yout, infil, rainw, rate, hsum, ssum, hmax};
+        R v[11] = {pp.acc_clip, pp.xin, pp.xout, pp.yin, pp.yout, pp.infil, pp.rainw, pp.rate, pp.hsum, pp.ssum,
+                   pp.hmax};
         const bool mx[11] = {false, false, false, false, false, false, false, true, false, false, true};
         const int sl[11] = {b, b + 1, b + 2, b + 3, b + 4, P_INFIL, P_RAINW, P_RATE, P_HSUM, P_SSUM, P_HMAX};
         block_reduce_store<11>(v, mx, red, out, sl, NT);

@@ -30,4 +30,8 @@ def main(ref_root: str) -> None:
 
 
 if __name__ == "__main__":
-    main(sys.argv[1] if len(sys.argv) > 1 else "/root/reference")
+    import os
+    root = sys.argv[1] if len(sys.argv) > 1 else os.environ.get("HIS_REFERENCE")
+    if not root:
+        raise SystemExit("usage: extract_suite_metrics.py <reference checkout>  (or set HIS_REFERENCE)")
+    main(root)

@@ -2,7 +2,7 @@
 
 Run in a container where the reference project is checked out:
 
-    PYTHONPATH=<reference checkout> python tests/golden/make_golden.py <reference checkout>
+    python tests/golden/make_golden.py <reference checkout> [group ...]
 
 It imports ``hydrointel`` from the given checkout, drives the reference's own
 SWE2D / SWE1D / exchange / CoupledEngine on small seeded cases and writes
@@ -215,21 +215,143 @@ def make_coupled_batch(name: str):
     print(name, "steps", spec["steps"], "final t", t, "n_sub max", max(rec["n_sub"]), "mass err", out["mass_err"])
 
 
+ASSEMBLY = {"lx_m": 4000.0, "ly_m": 3200.0, "cell_m": 80.0, "seed": 7, "steps": 800,
+            # (return period, rcp, ssp, horizon year, tide on, storm-tide offset h) per member
+            "scenarios": [(25, "RCP4.5", "SSP2", 2050, True, 0.0), (100, "RCP8.5", "SSP5", 2080, True, -2.0)]}
+
+
+def _store_forcing(out: dict, tag: str, fo) -> None:
+    out[f"{tag}rain_step"], out[f"{tag}rain_t0"] = fo.rain.step_s, fo.rain.t_start
+    out[f"{tag}rain_mmh"] = np.asarray(fo.rain.intensity_mmh, np.float64)
+    out[f"{tag}q_step"], out[f"{tag}q_t0"] = fo.inflow.step_s, fo.inflow.t0
+    out[f"{tag}q"] = np.asarray(fo.inflow.q_m3s, np.float64)
+    cons = list(fo.tide.cfg.constituents.values())
+    for k in ("amp_m", "period_h", "phase_deg"):
+        out[f"{tag}tide_{k}"] = np.array([c[k] for c in cons], np.float64)
+    out[f"{tag}tide_msl"], out[f"{tag}tide_slr"] = fo.tide.cfg.msl_offset_m, fo.tide.slr_m
+    out[f"{tag}tide_on"], out[f"{tag}tide_shift"] = float(fo.tide.on), fo.tide.shift_s
+    out[f"{tag}storm_start"], out[f"{tag}t_end"] = fo.storm_start, fo.t_end
+    out[f"{tag}drainage"] = fo.ssp.drainage_investment_factor
+    ts = np.linspace(0.0, fo.t_end, 97)
+    out[f"{tag}sample_t"] = ts
+    out[f"{tag}sample_rain"] = np.array([fo.rain.rate_ms(t) for t in ts])
+    out[f"{tag}sample_tide"] = np.array([fo.tide(t) for t in ts])
+    out[f"{tag}sample_inflow"] = np.array([fo.inflow(t) for t in ts])
+
+
+def _run_recorded(eng, t_end: float, steps: int, out: dict, tag: str) -> None:
+    """Drive a reference CoupledEngine on its own CFL choice, recording dt and n_sub."""
+    dts, subs = [], []
+    t = 0.0
+    for _ in range(steps):
+        dt = min(eng.two.max_dt(), t_end - t)
+        n_sub = max(1, math.ceil(dt / eng.one.max_dt() - 1e-9))
+        dts.append(dt)
+        subs.append(n_sub)
+        t = eng.step(t, t_end, dt=dt, n_sub=n_sub)
+    out[f"{tag}dt"], out[f"{tag}n_sub"] = np.array(dts), np.array(subs)
+    for f in ("h", "hu", "hv", "s_filled", "infil_cum"):
+        out[f"{tag}{f}_end"] = _t(getattr(eng.two, f))
+    out[f"{tag}A_end"], out[f"{tag}Q_end"] = _t(eng.one.A), _t(eng.one.Q)
+    for k, v in eng.mb.sources().items():
+        out[f"{tag}src_{k}"] = np.asarray(v, np.float64)
+
+
+def make_assembly():
+    """The reference's own engine assembly (hydrointel/engine.py:169-238) on a small
+    generated domain: build_engine for one scenario and build_engine_batch for two, each
+    run 800 steps (past the storm start at 1800 s); the inputs are stored as plain arrays so the assembly can be rebuilt
+    without the reference."""
+    import dataclasses
+    import torch
+    from hydrointel.config import DomainConfig, RunConfig
+    from hydrointel.domain import landuse as LU
+    from hydrointel.domain.synthetic import generate
+    from hydrointel.engine import build_engine, build_engine_batch, build_forcing
+    A = ASSEMBLY
+    cfg = RunConfig()
+    cfg.solver.compile = False
+    cfg.domain = dataclasses.replace(cfg.domain, lx_m=A["lx_m"], ly_m=A["ly_m"], cell_m=A["cell_m"])
+    dom = generate(cfg.domain, A["seed"])
+    area = dom.nx * dom.ny * dom.dx ** 2 / 1e6
+    out = {"dem2d": dom.dem2d.astype(np.float64), "dx": dom.dx, "sea": dom.sea.astype(bool),
+           "landuse": dom.landuse.astype(np.int64), "inflow_reach": str(dom.network.inflow_reach)}
+    for k in ("f0_mmh", "fc_mmh", "k_per_h"):
+        out[f"lu_{k}"] = LU.table_array(k)
+    out["n_reaches"], out["n_junctions"] = dom.network.n_reaches, len(dom.network.junctions)
+    for i, r in enumerate(dom.network.reaches):
+        for k in ("x", "y", "bed", "width", "side_slope", "manning", "z_bank"):
+            out[f"reach{i}_{k}"] = np.asarray(getattr(r, k), np.float64)
+        out[f"reach{i}_id"] = str(r.reach_id)
+        out[f"reach{i}_up"] = np.array([str(v) for v in r.up])
+        out[f"reach{i}_down"] = np.array([str(v) for v in r.down])
+    for j, jn in enumerate(dom.network.junctions):
+        out[f"junction{j}"] = np.array([jn.x, jn.y, jn.bed, jn.width, jn.side_slope, jn.manning, jn.z_bank,
+                                        jn.length])
+    members = []
+    for m, sc in enumerate(A["scenarios"]):
+        rng = np.random.default_rng(100 + m)
+        lu = dom.landuse
+        storage = LU.lookup(lu, "storage_m") * rng.uniform(0.5, 1.5)
+        kappa = np.full(dom.shape, rng.uniform(0.7, 1.3))
+        manning = LU.lookup(lu, "manning") * rng.uniform(0.8, 1.2)
+        gamma = rng.uniform(0.8, 1.2, dom.network.n_reaches)
+        fo = build_forcing(cfg, sc[0], sc[1], sc[2], sc[3], sc[4], sc[5], area)
+        members.append((fo, storage, kappa, manning, gamma, lu))
+        out[f"m{m}_storage"], out[f"m{m}_kappa"], out[f"m{m}_manning"], out[f"m{m}_gamma"] = \
+            storage, kappa, manning, gamma
+        _store_forcing(out, f"m{m}_", fo)
+    cpu = torch.device("cpu")
+    # one scenario
+    fo, storage, kappa, manning, gamma, lu = members[0]
+    eng = build_engine(cfg, dom, fo, storage, kappa, manning, gamma, landuse=lu, device=cpu)
+    out["single_h0"], out["single_A0"] = _t(eng.two.h), _t(eng.one.A)
+    out["single_level0"] = _t(eng.one.level())
+    out["single_f0"], out["single_fc"], out["single_k"] = (_t(getattr(eng.two.horton, f)) for f in ("f0", "fc",
+                                                                                                   "k"))
+    _run_recorded(eng, fo.t_end, A["steps"], out, "single_")
+    # both scenarios as one batch
+    cols = list(zip(*members))
+    engb, _ = build_engine_batch(cfg, dom, list(cols[0]), list(cols[1]), list(cols[2]), list(cols[3]),
+                                 list(cols[4]), list(cols[5]), device=cpu)
+    out["batch_h0"], out["batch_A0"] = _t(engb.two.h), _t(engb.one.A)
+    _run_recorded(engb, members[0][0].t_end, A["steps"], out, "batch_")
+    np.savez_compressed(HERE / "assembly_run.npz", **out)
+    print("assembly_run", dom.ny, "x", dom.nx, "reaches", dom.network.n_reaches, "junctions",
+          len(dom.network.junctions), "dt", out["single_dt"][[0, -1]], "n_sub max", out["single_n_sub"].max())
+
+
+def reference_checkout(argv) -> Path:
+    """The reference checkout: the first argument, else $HIS_REFERENCE; required."""
+    import os
+    root = argv[1] if len(argv) > 1 else os.environ.get("HIS_REFERENCE")
+    if not root:
+        raise SystemExit("usage: make_golden.py <reference checkout> [group ...]  (or set HIS_REFERENCE); "
+                         "groups: swe2d swe1d exchange coupled coupled_batch assembly")
+    root = Path(root)
+    if not (root / "hydrointel").is_dir():
+        raise SystemExit(f"{root} is not a checkout of the reference (no hydrointel/ package)")
+    return root
+
+
 def main(argv):
-    ref = Path(argv[1] if len(argv) > 1 else "/root/reference")
+    ref = reference_checkout(argv)
     sys.path.insert(0, str(ref))
     import torch
     torch.set_num_threads(1)
-    for name in GC.SWE2D_CASES:
-        make_swe2d(name, ref)
-    for name in GC.SWE1D_CASES:
-        make_swe1d(name)
-    for name in GC.EXCHANGE_CASES:
-        make_exchange(name)
-    for name in GC.COUPLED_CASES:
-        make_coupled(name)
-    for name in GC.COUPLED_BATCH_CASES:
-        make_coupled_batch(name)
+    groups = {
+        "swe2d": lambda: [make_swe2d(n, ref) for n in GC.SWE2D_CASES],
+        "swe1d": lambda: [make_swe1d(n) for n in GC.SWE1D_CASES],
+        "exchange": lambda: [make_exchange(n) for n in GC.EXCHANGE_CASES],
+        "coupled": lambda: [make_coupled(n) for n in GC.COUPLED_CASES],
+        "coupled_batch": lambda: [make_coupled_batch(n) for n in GC.COUPLED_BATCH_CASES],
+        "assembly": make_assembly,
+    }
+    chosen = argv[2:] or list(groups)
+    for g in chosen:
+        if g not in groups:
+            raise SystemExit(f"unknown group {g!r}; groups: {' '.join(groups)}")
+        groups[g]()
 
 
 if __name__ == "__main__":

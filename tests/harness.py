@@ -156,3 +156,42 @@ def oracle_from_storm(storm, cfg: SolverConfig | None = None):
     links = OracleLinks(cell1d, tp.zbank[cell1d], np.full(len(cell1d), length), ter.z.reshape(-1)[cells2d], inv,
                         uniq)
     return OracleCoupled(two, one, links, cfg, rain=f.rain_rate)
+
+
+def assembly_inputs(fx: dict):
+    """The inputs of the reference's engine assembly (hydrointel/engine.py:169-238),
+    rebuilt from the assembly fixture as plain stand-ins with the attributes the
+    assembly reads: run configuration, domain (bed, sea mask, land use, channel
+    network) and per member the scenario forcing and fields (storage, kappa,
+    roughness, channel gamma).  Returns (cfg, domain, members, landuse table)."""
+    import torch
+    from his_gb300.channels import ChannelNetwork, Junction, Reach
+    from his_gb300.config import SolverConfig
+    NS = SimpleNamespace
+    reaches = []
+    for i in range(int(fx["n_reaches"])):
+        g = lambda k: fx[f"reach{i}_{k}"]
+        end = lambda a: tuple(int(v) if v.lstrip("-").isdigit() else str(v) for v in a)
+        reaches.append(Reach(str(g("id")), g("x"), g("y"), g("bed"), g("width"), g("side_slope"), g("manning"),
+                             g("z_bank"), end(g("up")), end(g("down"))))
+    junctions = [Junction(*(float(v) for v in fx[f"junction{j}"])) for j in range(int(fx["n_junctions"]))]
+    net = ChannelNetwork(reaches, junctions, str(fx["inflow_reach"]))
+    domain = NS(dem2d=fx["dem2d"], dx=float(fx["dx"]), sea=fx["sea"], landuse=fx["landuse"], network=net)
+    cfg = NS(solver=SolverConfig(), dtype=torch.float64)
+    members = []
+    m = 0
+    while f"m{m}_rain_mmh" in fx:
+        g = lambda k: fx[f"m{m}_{k}"]
+        cons = {f"c{j}": {"amp_m": float(a), "period_h": float(p), "phase_deg": float(ph)}
+                for j, (a, p, ph) in enumerate(zip(g("tide_amp_m"), g("tide_period_h"), g("tide_phase_deg")))}
+        forcing = NS(rain=NS(step_s=float(g("rain_step")), intensity_mmh=g("rain_mmh"), t_start=float(g("rain_t0"))),
+                     inflow=NS(step_s=float(g("q_step")), q_m3s=g("q"), t0=float(g("q_t0"))),
+                     tide=NS(cfg=NS(constituents=cons, msl_offset_m=float(g("tide_msl"))), slr_m=float(g("tide_slr")),
+                             on=bool(g("tide_on")), shift_s=float(g("tide_shift"))),
+                     storm_start=float(g("storm_start")), t_end=float(g("t_end")),
+                     ssp=NS(drainage_investment_factor=float(g("drainage"))))
+        members.append(NS(forcing=forcing, storage=g("storage"), kappa=g("kappa"), manning=g("manning"),
+                          gamma=g("gamma"), landuse=fx["landuse"]))
+        m += 1
+    table = {k: fx[f"lu_{k}"] for k in ("f0_mmh", "fc_mmh", "k_per_h")}
+    return cfg, domain, members, table

@@ -48,10 +48,53 @@ def test_plain_full_1000_steps_match_oracle():
     for term, v in orc.acc.items():
         assert src[term] == pytest.approx(float(v[0]), rel=1e-9, abs=1e-6), term
     assert eng.mb.check(eng.total_volume(), t, record=False) < 1e-3
-    # what the 1000 steps exercised
-    assert orc.exch[0, 0] > 0 and orc.exch[0, 1] > 0, "weir exchange in both directions"
+    # what the first 1000 steps exercise (the weir links start later: see the next test)
     assert src["infiltration"] > 0 and src["rain"] > 0 and src["bnd2d_in"] > 0 and src["bnd1d_out"] > 0
     assert float(orc.two.s_filled.max()) > 0, "retention store filled"
+
+
+def test_plain_full_mid_storm_1000_steps_match_oracle():
+    """The same storm from t = 5400 s (1.5 h, rising limb: the channel overtops into the
+    floodplain and the floodplain drains back over other banks): the CUDA float64 engine
+    runs there on its own CFL steps, the oracle takes over its state, and both then take
+    1000 steps on the oracle's dt and substep sequence.  Same bounds as from t = 0, on
+    the states and on the volume terms accumulated over the 1000 steps; the weir links
+    move water in both directions."""
+    from his_gb300 import workloads as W
+    from his_gb300.assembly import build_engine
+    from his_gb300.massbalance import TERMS
+    storm = W.plain_full()
+    eng = build_engine(storm)
+    t = 0.0
+    while t < 5400.0:
+        t = eng.step(t, storm.t_end)
+    orc = H.oracle_from_storm(storm)
+    for f in ("h", "hu", "hv", "s_filled", "infil_cum"):
+        getattr(orc.two, f)[0][...] = _np(getattr(eng.two, f))
+    orc.one.A[0][...] = _np(eng.one.A)
+    orc.one.Q[0][...] = _np(eng.one.Q)
+    src0 = eng.mb.sources()
+    t0 = t
+    for _ in range(1000):
+        dt = min(orc.two.max_dt(), storm.t_end - t)
+        n_sub = max(1, int(np.ceil(dt / orc.one.max_dt() - 1e-9)))
+        orc.step(t, storm.t_end, dt=dt, n_sub=n_sub)
+        t = eng.step(t, storm.t_end, dt=dt, n_sub=n_sub)
+    d = {f: H.max_abs(_np(getattr(eng.two, f)), getattr(orc.two, f)[0]) for f in ("h", "hu", "hv")}
+    dA = H.max_abs(_np(eng.one.A), orc.one.A[0])
+    dQ = H.max_abs(_np(eng.one.Q), orc.one.Q[0])
+    src = eng.mb.sources()
+    inc = {k: src[k] - src0[k] for k in TERMS}
+    print(f"t {t0:.1f} -> {t:.1f} s: " + ", ".join(f"|d{k}| {v:.3e}" for k, v in d.items()) +
+          f", |dA| {dA:.3e}, |dQ| {dQ:.3e}; exchanged 2-D->1-D {orc.exch[0, 0]:.1f} m^3, 1-D->2-D "
+          f"{orc.exch[0, 1]:.1f} m^3 over {int(orc.links_active.sum())}/{orc.links.n_links} links; "
+          f"terms over the segment {inc}")
+    assert d["h"] <= 1e-9 and d["hu"] <= 1e-9 and d["hv"] <= 1e-9
+    assert dA <= 1e-8 and dQ <= 1e-8
+    for term, v in orc.acc.items():
+        assert inc[term] == pytest.approx(float(v[0]), rel=1e-9, abs=1e-6), term
+    assert orc.exch[0, 0] > 0 and orc.exch[0, 1] > 0, "weir exchange in both directions"
+    assert eng.mb.check(eng.total_volume(), t, record=False) < 1e-3
 
 
 def test_fp32_against_fp64_full_resolution_members():
