@@ -35,27 +35,27 @@ struct alignas(4 * sizeof(R)) Q4 {
     R a, b, c, d;
 };
 
-// Shared-memory layout of one CTA.  Only what a neighbouring thread reads lives here
-// (cells of the rows around the x-reconstruction, the plus side of each x-
-// reconstruction, x-faces and theta); a thread's own column -- its cells, y-faces,
-// thetas and bed terms -- is carried in registers from row to row.  Every array has
-// one padding slot on each side: thread t's entry is at t + 1, so the neighbours of
-// the first and last thread are in bounds (their values are never used).
+// Shared-memory layout of one CTA.  Rings of the last rows' cells, x- and y-faces and
+// thetas: a thread publishes each value once and reads both its neighbours' entries
+// and its own earlier rows from them, so no row-to-row state is shifted through
+// registers.  Every row of entries has one padding slot on each side: thread t's
+// entry is at t + 1, so the neighbours of the first and last thread are in bounds
+// (their values are never used).
 template <class R, int NT>
 struct StripGeom {
-    static constexpr int RING = 4;                 // cell rows kept (rows r-2 .. r are read)
+    static constexpr int RING = 4;                 // rows kept per ring (slot = row & 3)
     static constexpr int P = NT + 2;               // padded row of entries
     static constexpr int NRED = 11;                // reduced values (the reduction reuses the cell ring)
-    // cells [RING][P], x-recon plus side [P], x-faces [2][P]; then plus-side surface
-    // slope [P] and theta [2][P]
-    static constexpr size_t quads = (size_t)(RING + 1 + 2) * P;
-    static constexpr size_t scalars = (size_t)(1 + 2) * P;
+    // cells [RING][P], x-recon plus side [P], x-faces [2][P], y-faces [RING][P]; then
+    // the plus-side surface slope [P] and theta [RING][P]
+    static constexpr size_t quads = (size_t)(RING + 1 + 2 + RING) * P;
+    static constexpr size_t scalars = (size_t)(1 + RING) * P;
     static_assert((size_t)4 * RING * P >= (size_t)(NT / 32) * NRED, "reduction scratch must fit in the cell ring");
     static constexpr size_t smem_bytes = sizeof(Q4<R>) * quads + sizeof(R) * scalars;
     // resident CTAs per SM the float32 kernels are register-capped for; float64 keeps
     // the compiler's choice (one CTA of any width must fit the register file)
     static constexpr int min_ctas(int stage) {
-        return sizeof(R) == 4 ? ((stage == 1 ? 640 : 512) / NT > 0 ? (stage == 1 ? 640 : 512) / NT : 1) : 1;
+        return sizeof(R) == 4 ? ((stage == 1 ? 768 : 640) / NT > 0 ? (stage == 1 ? 768 : 640) / NT : 1) : 1;
     }
 };
 
@@ -258,16 +258,14 @@ __device__ __forceinline__ Q4<R> side_flux(const KC<R>& c, const Side<R>& L, R z
 
 // The row-marching pipeline of one strip chunk (see the head of this file).  Row r is
 // the newest row built; per row two barriers separate the phases:
-//   A  build row r into the ring, prefetch row r+2 and the update inputs of row r-3;
-//      y-reconstruction of row r-1 and the y-face between rows r-2 and r-1 (own
-//      column, registers); x-reconstruction of row r-2 (neighbours from the ring),
-//      its plus side published for the next thread
+//   A  build row r into the cell ring, prefetch row r+1 and the update inputs of row
+//      r-3; y-reconstruction of row r-1 and the y-face between rows r-2 and r-1;
+//      x-reconstruction of row r-2 from its neighbours' cells, plus side published
 //   -- barrier --
-//   B  x-face between columns cx-1 and cx of row r-2, published for thread t-1
+//   B  x-face between columns cx-1 and cx of row r-2, published
 //   -- barrier --
-//   C  theta of row r-2, published for the neighbours
-//   D  update of row r-3: its own fluxes and thetas from registers, the east face and
-//      the west / east thetas from the previous row's shared entries
+//   C  theta of row r-2, published
+//   D  update of row r-3 from the rings' entries of rows r-4 .. r-2
 // row<true> is the steady state: every row touched lies inside the grid, so the
 // range tests, y-ghosts and domain-edge terms drop out; row<false> handles the
 // pipeline fill at the chunk's start, the drain at its end and the grid's edges.
@@ -275,9 +273,11 @@ template <class R, int NT, int STAGE>
 struct StripPipe {
     using G = StripGeom<R, NT>;
     static constexpr int P = G::P;
+    static constexpr int RM = G::RING - 1;
     Q4<R>* s_cell;
     Q4<R>* s_rp;
     Q4<R>* s_xf;
+    Q4<R>* s_yf;
     R* s_rs;
     R* s_th;
     const Grid<R>& gd;
@@ -287,17 +287,12 @@ struct StripPipe {
     const R* __restrict__ H;
     const R* __restrict__ HU;
     const R* __restrict__ HV;
-    int t, ts, cx, cxc, nx, ny, y0, y1, scol, xside, xkind;
+    int ts, cx, cxc, nx, ny, y0, y1, scol, xside, xkind;
     bool col_in, do_out, west, east;
     R dt, rdx, rdy, idx, idy, rdt, tt;
     // carried state of this thread's column
-    HaloRaw<R> ra, rb;                 // raw rows r+1 and r+2 (prefetched)
-    Q4<R> c1, c2;                      // cells of rows r-1 and r-2 {h, u, v, z}
-    R h3;                              // depth of row r-3
+    HaloRaw<R> ra;                     // raw row r (prefetched one row ahead)
     Side<R> ylow;                      // plus side of the y-reconstruction of row r-2
-    Q4<R> yf1, yf2;                    // y-faces r-2 and r-3
-    Q4<R> xf1;                         // own x-face of row r-3
-    R th1, th2;                        // theta of rows r-3 and r-4
     R by1, by2, bx1;                   // bed terms: y of rows r-2, r-3; x of row r-3
     CellIn<R> cin;
     R acc_clip, xin, xout, yin, yout, infil, rainw, rate, hsum, ssum, hmax;
@@ -326,7 +321,8 @@ struct StripPipe {
 
     template <bool FULL>
     __device__ __forceinline__ void row(const int r) {
-        const int s0 = (r & (G::RING - 1)) * P, s2 = ((r - 2) & (G::RING - 1)) * P;
+        const int k0 = (r & RM) * P, k1 = ((r - 1) & RM) * P, k2 = ((r - 2) & RM) * P, k3 = ((r - 3) & RM) * P,
+                  k4 = ((r - 4) & RM) * P;
         const int xo = ((r - 2) & 1) * P, xp = ((r - 3) & 1) * P;
         const int orow = r - 3, row = r - 2;
         const bool upd = FULL || (orow >= y0 && orow < y1);
@@ -337,17 +333,19 @@ struct StripPipe {
         } else {
             halo_build(c, gd, bcv, ra, cx, r, c0.a, c0.b, c0.c, c0.d);
         }
-        s_cell[s0 + ts] = c0;
-        ra = rb;
-        rb = FULL ? fetch_in(r + 2) : halo_fetch(c, gd, H, HU, HV, cx, r + 2);
+        s_cell[k0 + ts] = c0;
+        ra = FULL ? fetch_in(r + 1) : halo_fetch(c, gd, H, HU, HV, cx, r + 1);
         if (upd) cin = cell_fetch<R, STAGE>(gd, (size_t)orow * nx + cxc);
-        Q4<R> yf0{R(0), R(0), R(0), R(0)};
         R by0 = R(0), bx0 = R(0);
+        Q4<R> yf0{R(0), R(0), R(0), R(0)};
+        const Q4<R> c2 = s_cell[k2 + ts];           // own cells of rows r-2 and r-1
         if (FULL || r >= y0 - 1) {
+            const Q4<R> c1 = s_cell[k1 + ts];
             // y-reconstruction of row r-1: normal velocity v, tangential u
             const Recon<R> yup = reconstruct(c, c2.a, c1.a, c0.a, c2.c, c1.c, c0.c, c2.b, c1.b, c0.b, c2.d, c1.d, c0.d);
             const int fy = r - 1;
             if (FULL || (r >= y0 && fy >= 0 && fy <= ny)) yf0 = side_flux(c, ylow, c2.d, c2.a, side_minus(yup), c1.d, c1.a);
+            if (FULL || r >= y0) s_yf[k1 + ts] = yf0;
             ylow = side_plus(yup);
             if (c.order == 2) by0 = bed_term(c, yup);
         }
@@ -355,8 +353,8 @@ struct StripPipe {
         Q4<R> cl;
         Side<R> xm;
         if (xact) {
-            cl = s_cell[s2 + ts - 1];
-            const Q4<R> cr = s_cell[s2 + ts + 1];
+            cl = s_cell[k2 + ts - 1];
+            const Q4<R> cr = s_cell[k2 + ts + 1];
             const Recon<R> xr = reconstruct(c, cl.a, c2.a, cr.a, cl.b, c2.b, cr.b, cl.c, c2.c, cr.c, cl.d, c2.d, cr.d);
             const Side<R> xp_ = side_plus(xr);
             s_rp[ts] = Q4<R>{xp_.H, xp_.U, xp_.V, xp_.X};
@@ -377,38 +375,33 @@ struct StripPipe {
         __syncthreads();
         // ---- C: theta of row r-2 (swe2d.py:259-264); 1 outside the grid
         R th0 = R(1);
+        Q4<R> yn{R(0), R(0), R(0), R(0)};          // y-face r-2: south of row r-2, north of row r-3
         if (FULL || r >= y0 + 1) {
+            yn = s_yf[k2 + ts];
             if (FULL || (unsigned)row < (unsigned)ny) {
-                const R Fw = xf0.a, Fe = s_xf[xo + ts + 1].a, Gs = yf1.a, Gn = yf0.a;
+                const R Fw = xf0.a, Fe = s_xf[xo + ts + 1].a, Gs = yn.a, Gn = yf0.a;
                 const R out = per_len(relu(Fe) + relu(-Fw), rdx, idx) + per_len(relu(Gn) + relu(-Gs), rdy, idy);
                 const R need = out * dt;
                 const R hh = c2.a;
                 const R th = need > hh ? hh / (need > R(0) ? need : R(1)) : R(1);
                 th0 = col_in ? th : R(1);
             }
-            s_th[xo + ts] = th0;
+            s_th[k2 + ts] = th0;
         }
         // ---- D: update of row r-3
-        if (upd) update<FULL>(orow, xp, th0);
-        // ---- shift the carried column
-        h3 = c2.a;
-        c2 = c1;
-        c1 = c0;
-        yf2 = yf1;
-        yf1 = yf0;
+        if (upd) update<FULL>(orow, xp, k3, k4, th0, yn);
         by2 = by1;
         by1 = by0;
         bx1 = bx0;
-        xf1 = xf0;
-        th2 = th1;
-        th1 = th0;
     }
 
     template <bool FULL>
-    __device__ __forceinline__ void update(const int orow, const int xp, const R thN) {
-        const R thC = th1, thS = th2;
-        const R thW = s_th[xp + ts - 1], thE = s_th[xp + ts + 1];
-        const Q4<R> xw = xf1, xe = s_xf[xp + ts + 1], ys = yf2, yn = yf1;
+    __device__ __forceinline__ void update(const int orow, const int xp, const int k3, const int k4, const R thN,
+                                           const Q4<R>& yn) {
+        const R thC = s_th[k3 + ts], thS = s_th[k4 + ts];
+        const R thW = s_th[k3 + ts - 1], thE = s_th[k3 + ts + 1];
+        const Q4<R> xw = s_xf[xp + ts], xe = s_xf[xp + ts + 1], ys = s_yf[k3 + ts];
+        const R h3 = s_cell[k3 + ts].a;
         const R Fw = xw.a, Fe = xe.a, Gs = ys.a, Gn = yn.a;
         const R sw = Fw > R(0) ? thW : thC, se = Fe > R(0) ? thC : thE;
         const R ss = Gs > R(0) ? thS : thC, sn = Gn > R(0) ? thC : thN;
@@ -592,15 +585,17 @@ __global__ void __launch_bounds__(NT, StripGeom<R, NT>::min_ctas(STAGE)) strip_k
     __syncthreads();
     const Grid<R>& gd = s_gd;
     Q4<R>* s_cell = reinterpret_cast<Q4<R>*>(smem_raw);
-    StripPipe<R, NT, STAGE> pp{s_cell, s_cell + G::RING * P, s_cell + (G::RING + 1) * P,
-                               reinterpret_cast<R*>(s_cell + (G::RING + 3) * P),
-                               reinterpret_cast<R*>(s_cell + (G::RING + 3) * P) + P, gd, c, bcv, s_snap,
+    Q4<R>* s_rp = s_cell + G::RING * P;
+    Q4<R>* s_xf = s_rp + P;
+    Q4<R>* s_yf = s_xf + 2 * P;
+    R* s_rs = reinterpret_cast<R*>(s_yf + G::RING * P);
+    R* s_th = s_rs + P;
+    StripPipe<R, NT, STAGE> pp{s_cell, s_rp, s_xf, s_yf, s_rs, s_th, gd, c, bcv, s_snap,
                                STAGE == 2 ? gd.h1 : gd.h, STAGE == 2 ? gd.hu1 : gd.hu, STAGE == 2 ? gd.hv1 : gd.hv};
     const int nx = gd.nx, ny = gd.ny;
     const int x0 = sr.x0, W = sr.w, y0 = sr.y0, y1 = sr.y1;
     const int cx = x0 - 3 + t;                        // this thread's column
     const int q = cx - x0;                            // column relative to the strip
-    pp.t = t;
     pp.ts = t + 1;
     pp.cx = cx;
     pp.cxc = cx < 0 ? 0 : (cx > nx - 1 ? nx - 1 : cx);
@@ -625,15 +620,12 @@ __global__ void __launch_bounds__(NT, StripGeom<R, NT>::min_ctas(STAGE)) strip_k
     pp.acc_clip = pp.xin = pp.xout = pp.yin = pp.yout = pp.infil = pp.rainw = pp.rate = pp.hsum = pp.ssum = R(0);
     pp.hmax = R(0);
     pp.by1 = pp.by2 = pp.bx1 = R(0);
-    pp.th1 = pp.th2 = R(1);
-    pp.h3 = R(0);
-    // software pipeline: raw rows are fetched two rows ahead
+    // software pipeline: raw rows are fetched one row ahead
     pp.ra = halo_fetch(c, gd, pp.H, pp.HU, pp.HV, cx, y0 - 3);
-    pp.rb = halo_fetch(c, gd, pp.H, pp.HU, pp.HV, cx, y0 - 2);
     static_assert((G::RING & (G::RING - 1)) == 0, "ring slots are row & (RING - 1)");
-    // steady-state rows: every row touched (r-4 .. r+2) inside the grid, the update row
+    // steady-state rows: every row touched (r-4 .. r+1) inside the grid, the update row
     // neither the first nor the last row of the grid
-    const int r_lo = max(y0 + 3, 4), r_hi = min(y1 + 2, ny - 3);
+    const int r_lo = max(y0 + 3, 4), r_hi = min(y1 + 2, ny - 2);
     int r = y0 - 3;
     for (; r <= y1 + 2 && r < r_lo; ++r) pp.template row<false>(r);
     for (; r <= r_hi; ++r) pp.template row<true>(r);
