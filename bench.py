@@ -360,18 +360,23 @@ def accuracy_c3_leg(members: int = 2, interval_s: float = 120.0) -> dict:
     (max and RMSE over wet cells), arrival time at 0.1 m from the outputs, volume and
     both runs' mass-balance errors."""
     from his_gb300 import workloads as W
-    from his_gb300.accuracy import against_fp64
+    from his_gb300.accuracy import against_fp64, reference_criteria
     w0 = time.perf_counter()
     rows = against_fp64(W.batched_uniform(members), interval_s)
     keep = ("member", "status_fp32", "status_fp64", "steps_fp32", "steps_fp64", "peak_depth_rmse_m",
             "peak_depth_max_m", "peak_every_step_rmse_m", "wet_cells", "arrival_rmse_s", "arrival_max_s",
             "arrival_cells", "arrival_cells_in_one_run_only", "final_volume_rel", "final_surface_volume_rel",
-            "mass_error_fp32", "mass_error_fp64")
+            "depth_rmse_wet_m", "depth_p99_abs_m", "depth_max_abs_m", "flooded_area_rel",
+            "reach_peak_discharge_rel", "mass_error_fp32", "mass_error_fp64")
+    crit = [reference_criteria(r) for r in rows]
     return {"workload": f"{members} members of the 64-storm batch, 400x325 @ 20 m, 8.5 h storms to their end, "
                         f"float32 production form against float64, outputs every {interval_s:.0f} s",
             "peak_depth_rmse_m_max": max(r["peak_depth_rmse_m"] for r in rows),
             "arrival_rmse_s_max": max(r["arrival_rmse_s"] for r in rows),
             "mass_error_fp32_max": max(r["mass_error_fp32"] for r in rows),
+            "reach_peak_discharge_rel_max": max(r.get("reach_peak_discharge_rel", 0.0) for r in rows),
+            "reference_fp32_criteria": {k: {"worst": max(c[k]["value"] for c in crit), "limit": crit[0][k]["limit"],
+                                            "pass_all": all(c[k]["pass"] for c in crit)} for k in crit[0]},
             "members": [{k: r[k] for k in keep if k in r} for r in rows],
             "wall_s": time.perf_counter() - w0}
 

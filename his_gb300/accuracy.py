@@ -35,6 +35,58 @@ def arrival_times(depth_series, times, threshold: float = 0.1) -> np.ndarray:
     return out
 
 
+# The reference's own acceptance criteria for a float32 run against float64
+# (hydrointel/benchmarks/precision.py:37-44 and criteria.py:40-46); reported beside
+# the comparison, the benchmark spec's bar being peak-depth RMSE <= 1 cm.
+REFERENCE_FP32_CRITERIA = {
+    "mass_balance_error": 1e-4,
+    "depth_max_abs_m": 5e-3,
+    "depth_rmse_wet_m": 1e-3,
+    "peak_depth_max_m": 5e-3,
+    "flooded_area_rel": 0.005,
+    "reach_peak_discharge_rel": 0.02,
+}
+AREA_THRESHOLDS_M = (0.15, 0.30, 0.50)
+
+
+def series_metrics(test, ref, reach_of=None, h_dry: float = 1e-3) -> dict:
+    """Output-series agreement in the reference's terms (criteria.py:25-33): depth RMSE
+    and 99th-percentile |dh| over every (output time, cell) wet in either run, the
+    largest |dh| anywhere, the flooded area (peak depth at 0.15 / 0.30 / 0.50 m, cells
+    dry at the start) relative to ``ref``, and per reach the peak of |Q| over time and
+    its nodes relative to ``ref`` (``reach_of``: reach index of each output node)."""
+    h_t, h_r = _np(test.depth_series), _np(ref.depth_series)
+    n = min(len(h_t), len(h_r))
+    h_t, h_r = h_t[:n], h_r[:n]
+    d = h_t - h_r
+    wet = np.maximum(h_t, h_r) > h_dry
+    out = {"depth_rmse_wet_m": float(np.sqrt(np.mean(d[wet] ** 2))) if wet.any() else 0.0,
+           "depth_p99_abs_m": float(np.percentile(np.abs(d[wet]), 99)) if wet.any() else 0.0,
+           "depth_max_abs_m": float(np.abs(d).max()) if d.size else 0.0}
+    land = (h_r[0] <= 0.0) & (h_t[0] <= 0.0) if n else None
+    rel_area = 0.0
+    if n:
+        pk_t, pk_r = h_t.max(axis=0), h_r.max(axis=0)
+        for thr in AREA_THRESHOLDS_M:
+            a_r = float(((pk_r >= thr) & land).sum())
+            a_t = float(((pk_t >= thr) & land).sum())
+            if a_r > 0:
+                rel_area = max(rel_area, abs(a_t - a_r) / a_r)
+    out["flooded_area_rel"] = rel_area
+    q_t, q_r = _np(test.channel_q)[:n], _np(ref.channel_q)[:n]
+    if reach_of is not None and q_r.size:
+        reach_of = np.asarray(reach_of)
+        worst = 0.0
+        for rch in np.unique(reach_of):
+            sel = reach_of == rch
+            p_r = float(np.abs(q_r[:, sel]).max())
+            p_t = float(np.abs(q_t[:, sel]).max())
+            if p_r > 0:
+                worst = max(worst, abs(p_t - p_r) / p_r)
+        out["reach_peak_discharge_rel"] = worst
+    return out
+
+
 def compare(test, ref, threshold: float = 0.1, wet: float = 1e-3) -> dict:
     """Errors of FloodResult ``test`` against FloodResult ``ref`` of the same storm.
 
@@ -92,6 +144,12 @@ def against_fp64(storms, interval_s: float, cfg=None, chunk: int = 1024, timeout
     for b, s in enumerate(storms):
         (f64, r64), (f32, r32) = (runs["fp64"][0][b], runs["fp64"][1][b]), (runs["fp32"][0][b], runs["fp32"][1][b])
         m = compare(f32, f64)
+        reach_of = None
+        if s.network is not None:
+            from .topology import build_topology
+            tp = build_topology(s.network)
+            reach_of = tp.reach_of[tp.kind <= 1]
+        m.update(series_metrics(f32, f64, reach_of))
         # the running maxima over every step, beside the maxima over the output times
         e32, e64 = f32.extras.get("depth_max_every_step"), f64.extras.get("depth_max_every_step")
         if e32 is not None and e64 is not None:
@@ -109,4 +167,14 @@ def against_fp64(storms, interval_s: float, cfg=None, chunk: int = 1024, timeout
     return out
 
 
-__all__ = ["arrival_times", "compare", "against_fp64"]
+def reference_criteria(m: dict) -> dict:
+    """Each of the reference's float32 acceptance criteria with its value in ``m`` and
+    whether it holds (mass balance judged on the float32 run)."""
+    vals = dict(m)
+    vals.setdefault("mass_balance_error", m.get("mass_error_fp32"))
+    return {k: {"value": vals.get(k), "limit": lim, "pass": vals.get(k) is not None and vals[k] <= lim}
+            for k, lim in REFERENCE_FP32_CRITERIA.items()}
+
+
+__all__ = ["arrival_times", "compare", "against_fp64", "series_metrics", "reference_criteria",
+           "REFERENCE_FP32_CRITERIA"]

@@ -28,6 +28,7 @@ UNITS = {
     "swe2d_f64.cu": ["-fmad=false"],
     "swe2d_f32.cu": ["-fmad=true", "--use_fast_math"],
     "net1d.cu": ["-fmad=false"],
+    "net1d_f32.cu": ["-fmad=true", "--use_fast_math"],
     "noalloc.cu": [],
 }
 

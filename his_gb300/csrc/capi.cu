@@ -380,7 +380,7 @@ int32_t his_net_create(const his_solver_cfg* cfg, int32_t n_members, const his_n
     if (n_members <= 0 || !nets) return bad("need at least one network member");
     Arena ar;
     struct Offs { size_t kind, gsrc, fl, fr, gsign, ls, li, rs, ri, z, n, dx, b, m, yb, ts, fb, fm, fyb, fts;
-                  size_t zf, dxf, bf, mf, ybf, tsf; };
+                  size_t zf, dxf, bf, mf, ybf, tsf, nf, gsf, fbf, fmf, fybf, ftsf; };
     std::vector<Offs> offs(n_members);
     size_t smem = 0;
     for (int mb = 0; mb < n_members; ++mb) {
@@ -418,13 +418,17 @@ int32_t his_net_create(const his_solver_cfg* cfg, int32_t n_members, const his_n
         o.z = ar.add(d.z, C); o.n = ar.add(d.manning, C); o.dx = ar.add(d.dx, C);
         o.b = ar.add(d.b, C); o.m = ar.add(d.m, C); o.yb = ar.add(d.yb, C); o.ts = ar.add(d.ts, C);
         o.fb = ar.add(d.fb, F); o.fm = ar.add(d.fm, F); o.fyb = ar.add(d.fyb, F); o.fts = ar.add(d.fts, F);
-        // float32 copies of the static cell geometry for the production form's exchange
-        auto addf = [&](const double* a) {
-            std::vector<float> f(a, a + d.n_cells);
+        // float32 copies of the static geometry for the production form's exchange and
+        // network substeps
+        auto addf = [&](const double* a, int n) {
+            std::vector<float> f(a, a + n);
             return ar.add(f.data(), sizeof(float) * f.size());
         };
-        o.zf = addf(d.z); o.dxf = addf(d.dx); o.bf = addf(d.b); o.mf = addf(d.m); o.ybf = addf(d.yb);
-        o.tsf = addf(d.ts);
+        o.zf = addf(d.z, d.n_cells); o.dxf = addf(d.dx, d.n_cells); o.bf = addf(d.b, d.n_cells);
+        o.mf = addf(d.m, d.n_cells); o.ybf = addf(d.yb, d.n_cells); o.tsf = addf(d.ts, d.n_cells);
+        o.nf = addf(d.manning, d.n_cells); o.gsf = addf(d.ghost_sign, d.n_cells);
+        o.fbf = addf(d.fb, d.n_faces); o.fmf = addf(d.fm, d.n_faces); o.fybf = addf(d.fyb, d.n_faces);
+        o.ftsf = addf(d.fts, d.n_faces);
         smem = std::max(smem, net_smem_bytes(d.n_cells, d.n_faces));
     }
     if (smem > 200 * 1024) return bad("network too large for one thread block's shared memory");
@@ -460,6 +464,9 @@ int32_t his_net_create(const his_solver_cfg* cfg, int32_t n_members, const his_n
         n.zf = (const float*)(base + o.zf); n.dxf = (const float*)(base + o.dxf);
         n.bf = (const float*)(base + o.bf); n.mf = (const float*)(base + o.mf);
         n.ybf = (const float*)(base + o.ybf); n.tsf = (const float*)(base + o.tsf);
+        n.nmanf = (const float*)(base + o.nf); n.gsignf = (const float*)(base + o.gsf);
+        n.fbf = (const float*)(base + o.fbf); n.fmf = (const float*)(base + o.fmf);
+        n.fybf = (const float*)(base + o.fybf); n.ftsf = (const float*)(base + o.ftsf);
         n.A = d.A; n.Q = d.Q;
     }
     e = cudaMalloc(&N->d_nets, sizeof(Net) * n_members);

@@ -180,5 +180,8 @@ int net_step_launch(his_net* n, double dt, int n_sub, cudaStream_t s, double* vo
 int net_reduce_launch(his_net* n, cudaStream_t s, double* rate_wet = nullptr);
 int net_engine_launch(his_engine* e, cudaStream_t s, int m0, int count);
 int net_engine_prepare(his_engine* e);
+// net1d_f32.cu: the float32 network of the production form (float32 engines)
+int net_engine_launch_f32(his_engine* e, cudaStream_t s, int m0, int count);
+int net_engine_prepare_f32(his_engine* e);
 
 }  // namespace his

@@ -1,4 +1,5 @@
-// Launchers of the 1-D network kernels (float64, built with -fmad=false).
+// Launchers of the 1-D network kernels (float64, built with -fmad=false); float32
+// engines run the production form's network (net1d_f32.cu).
 #include "his_internal.h"
 #include "net1d_kernels.cuh"
 
@@ -66,6 +67,7 @@ __global__ void net_engine_kernel(const Net* __restrict__ nets, Consts c, const 
 }
 
 int net_engine_prepare(his_engine* e) {
+    if (e->grid->prec == HIS_PREC_F32) return net_engine_prepare_f32(e);
     if (e->net && e->net->smem > 48 * 1024)
         HIS_CK(cudaFuncSetAttribute(net_engine_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                     (int)e->net->smem));
@@ -73,6 +75,7 @@ int net_engine_prepare(his_engine* e) {
 }
 
 int net_engine_launch(his_engine* e, cudaStream_t s, int m0, int count) {
+    if (e->grid->prec == HIS_PREC_F32) return net_engine_launch_f32(e, s, m0, count);
     his_net* n = e->net;
     net_engine_kernel<<<count, 128, n->smem, s>>>(n->d_nets, n->c, e->d_em, e->grid->d_params, e->d_netf, e->max_sub,
                                                   e->d_vol1d, m0);

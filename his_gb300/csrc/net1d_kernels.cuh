@@ -28,6 +28,8 @@ struct Net {
     const double *b, *m, *yb, *ts;                 // cell sections
     const double *fb, *fm, *fyb, *fts;             // face sections
     const float *zf, *dxf, *bf, *mf, *ybf, *tsf;   // float32 copies of z, dx and the cell sections
+    const float *nmanf, *gsignf;                   // float32 roughness and ghost signs
+    const float *fbf, *fmf, *fybf, *ftsf;          // float32 face sections
     double *A, *Q;
 };
 
@@ -267,6 +269,229 @@ __device__ __forceinline__ void net_substeps_dev(const Net& N, const Consts& c, 
     }
 }
 
+
+// ---------------------------------------------------------- float32 substeps
+// The production form of the network step: section geometry, wave speeds, fluxes,
+// the outflow limiter and friction in float32 arithmetic; the state (cross-section
+// area A and discharge Q), its per-substep update, the clip and boundary tallies, and
+// the depth of the junction level pools in float64.  GB300 runs float64 at a small
+// fraction of its float32 rate, and the float64 network filled one SM's float64 pipe.
+struct SecF {
+    const float *b, *m, *yb, *ts;
+};
+__device__ __forceinline__ float secf_area(const SecF& s, int i, float y) {
+    const float yt = fminf(y, s.yb[i]);
+    return yt * (s.b[i] + s.m[i] * yt) + s.ts[i] * fmaxf(y - s.yb[i], 0.0f);
+}
+__device__ __forceinline__ float secf_top(const SecF& s, int i, float y) {
+    return y <= s.yb[i] ? s.b[i] + 2.0f * s.m[i] * y : s.ts[i];
+}
+__device__ __forceinline__ float secf_i1(const SecF& s, int i, float y) {
+    const float yt = fminf(y, s.yb[i]);
+    const float above = fmaxf(y - s.yb[i], 0.0f);
+    const float it = s.b[i] * yt * yt * 0.5f + s.m[i] * (yt * yt * yt) * (1.0f / 3.0f);
+    const float at = yt * (s.b[i] + s.m[i] * yt);
+    return it + at * above + s.ts[i] * above * above * 0.5f;
+}
+__device__ __forceinline__ float secf_perim(const SecF& s, int i, float y) {
+    const float yt = fminf(y, s.yb[i]);
+    return s.b[i] + 2.0f * yt * sqrtf(1.0f + s.m[i] * s.m[i]);
+}
+__device__ __forceinline__ float secf_depth(const SecF& s, int i, float A) {
+    A = fmaxf(A, 0.0f);
+    const float b = s.b[i], yb = s.yb[i];
+    const float ab = yb * (b + s.m[i] * yb);
+    return A <= ab ? 2.0f * A / (b + sqrtf(b * b + 4.0f * s.m[i] * A)) : yb + (A - ab) / s.ts[i];
+}
+
+__device__ __forceinline__ void hll_1d_f32(float AL, float QL, float pL, float cL, float AR, float QR, float pR,
+                                           float cR, float uL, float uR, float& F1o, float& F2o) {
+    const float tiny = 1e-14f;
+    const bool dryL = AL <= tiny, dryR = AR <= tiny;
+    float SL = fminf(uL - cL, uR - cR);
+    float SR = fmaxf(uL + cL, uR + cR);
+    if (dryL) { SL = uR - 2.0f * cR; SR = uR + cR; }
+    if (dryR) { SL = uL - cL; SR = uL + 2.0f * cL; }
+    const float FL2 = QL * uL + pL, FR2 = QR * uR + pR;
+    float den = SR - SL;
+    if (fabsf(den) < tiny) den = 1.0f;
+    float F1, F2;
+    if (SL >= 0.0f) { F1 = QL; F2 = FL2; }
+    else if (SR <= 0.0f) { F1 = QR; F2 = FR2; }
+    else {
+        const float inv = 1.0f / den;
+        F1 = (SR * QL - SL * QR + SL * SR * (AR - AL)) * inv;
+        F2 = (SR * FL2 - SL * FR2 + SL * SR * (QR - QL)) * inv;
+    }
+    if (dryL && dryR) { F1 = 0.0f; F2 = 0.0f; }
+    F1o = F1;
+    F2o = F2;
+}
+
+__host__ __device__ inline size_t net_smem_bytes_f32(int n_cells, int n_faces) {
+    return sizeof(double) * (4 * (size_t)n_cells + 32 * 4) + sizeof(float) * (4 * (size_t)n_cells + 4 * (size_t)n_faces);
+}
+
+// n_sub substeps of dt/n_sub each for the network N (the arguments of net_substeps_dev).
+__device__ __forceinline__ void net_substeps_f32_dev(const Net& N, const Consts& c, double dt_total, int n_sub,
+                                                     const double* __restrict__ forcing, double* vols, double* sm,
+                                                     float* snap_eta = nullptr, float* snap_q = nullptr,
+                                                     double* snap_v1d = nullptr) {
+    const int nc = N.n_cells, nf = N.n_faces, tid = threadIdx.x, nt = blockDim.x;
+    double *A = sm, *Q = A + nc, *Ag = Q + nc, *Qg = Ag + nc, *red = Qg + nc;      // red: 128 doubles
+    float *Af = reinterpret_cast<float*>(red + 32 * 4), *yv = Af + nc, *uv = yv + nc, *th = uv + nc;
+    float *F1 = th + nc, *F2 = F1 + nf, *pL = F2 + nf, *pR = pL + nf;
+    const SecF s{N.bf, N.mf, N.ybf, N.tsf}, fs{N.fbf, N.fmf, N.fybf, N.ftsf};
+    const Sec sd{N.b, N.m, N.yb, N.ts};
+    __shared__ float s_k[3];
+    if (tid == 0) {
+        s_k[0] = (float)c.g;
+        s_k[1] = (float)c.h_dry;
+        s_k[2] = (float)(dt_total / n_sub);
+    }
+    for (int i = tid; i < nc; i += nt) { A[i] = N.A[i]; Q[i] = N.Q[i]; }
+    __syncthreads();
+    const float g = s_k[0], h_dry = s_k[1], dt = s_k[2];
+    double tot_in = 0.0, tot_out = 0.0, tot_clip = 0.0;
+    for (int k = 0; k < n_sub; ++k) {
+        const float q_in = (float)forcing[2 * k + 0];
+        const float eta = (float)forcing[2 * k + 1];
+        // ghost cells from the interior neighbour (swe1d.py:265-294)
+        for (int i = tid; i < nc; i += nt) {
+            const int kd = N.kind[i];
+            if (kd < 2) {
+                Ag[i] = A[i];
+                Qg[i] = Q[i];
+                Af[i] = (float)A[i];
+                continue;
+            }
+            const int src = N.gsrc[i];
+            const float As = (float)A[src], Qs = (float)Q[src], sg = N.gsignf[i];
+            const float ys = secf_depth(s, i, As);
+            const float un = sg * (ys >= h_dry ? Qs / fmaxf(As, 1e-12f) : 0.0f);
+            const bool wet_i = ys >= h_dry;
+            float An, Qn;
+            if (kd == 3) {
+                const float yst = fmaxf(eta - N.zf[i], 0.0f);
+                float Ast = secf_area(s, i, yst);
+                const float ci = sqrtf(g * As / secf_top(s, i, ys));
+                const float cg = sqrtf(g * Ast / secf_top(s, i, yst));
+                float un_st = wet_i ? un + 2.0f * (ci - cg) : 0.0f;
+                if (wet_i && (un > ci)) { un_st = un; Ast = As; }
+                if (!(secf_depth(s, i, Ast) >= h_dry)) un_st = 0.0f;
+                An = Ast;
+                Qn = sg * Ast * un_st;
+            } else if (kd == 2) {
+                const float b = N.bf[i];
+                const float yc = fmaxf(cbrtf(q_in * q_in / (g * b * b)), h_dry);
+                An = wet_i ? As : secf_area(s, i, yc);
+                Qn = -sg * q_in;
+            } else {
+                An = As;
+                Qn = -Qs;
+            }
+            Ag[i] = (double)An;
+            Qg[i] = (double)Qn;
+            Af[i] = An;
+        }
+        __syncthreads();
+        // depth and velocity; a junction's level-pool depth in float64
+        for (int i = tid; i < nc; i += nt) {
+            const float y = N.kind[i] == 1 ? (float)sec_depth(sd, i, Ag[i]) : secf_depth(s, i, Af[i]);
+            yv[i] = y;
+            uv[i] = y >= h_dry ? (float)Qg[i] / fmaxf(Af[i], 1e-12f) : 0.0f;
+        }
+        __syncthreads();
+        // face fluxes with hydrostatic reconstruction (swe1d.py:326-336)
+        for (int f = tid; f < nf; f += nt) {
+            const int l = N.fl[f], r = N.fr[f];
+            const float zL = N.zf[l], zR = N.zf[r], zfc = fmaxf(zL, zR);
+            const float yL = fmaxf(zL + yv[l] - zfc, 0.0f), yR = fmaxf(zR + yv[r] - zfc, 0.0f);
+            const float AL = secf_area(fs, f, yL), AR = secf_area(fs, f, yR);
+            const float uL = uv[l], uR = uv[r];
+            const float pl = g * secf_i1(fs, f, yL), pr = g * secf_i1(fs, f, yR);
+            pL[f] = pl;
+            pR[f] = pr;
+            const float cL = sqrtf(g * AL / secf_top(fs, f, yL));
+            const float cR = sqrtf(g * AR / secf_top(fs, f, yR));
+            hll_1d_f32(AL, AL * uL, pl, cL, AR, AR * uR, pr, cR, uL, uR, F1[f], F2[f]);
+        }
+        __syncthreads();
+        // outflow limiter; ghosts unlimited (swe1d.py:337-344)
+        for (int i = tid; i < nc; i += nt) {
+            float out = 0.0f;
+            for (int j = N.lstart[i]; j < N.lstart[i + 1]; ++j) out += fmaxf(F1[N.lidx[j]], 0.0f);
+            for (int j = N.rstart[i]; j < N.rstart[i + 1]; ++j) out += fmaxf(-F1[N.ridx[j]], 0.0f);
+            const float vol = Af[i] * N.dxf[i];
+            const float need = out * dt;
+            const float t = need > vol ? vol / (need > 0.0f ? need : 1.0f) : 1.0f;
+            th[i] = N.kind[i] >= 2 ? 1.0f : t;
+        }
+        __syncthreads();
+        double bsum[3] = {0.0, 0.0, 0.0};
+        for (int f = tid; f < nf; f += nt) {
+            const float sc = F1[f] > 0.0f ? th[N.fl[f]] : th[N.fr[f]];
+            const float Fs = F1[f] * sc;
+            F1[f] = Fs;
+            if (N.kind[N.fl[f]] >= 2) { bsum[0] += fmaxf(Fs, 0.0f); bsum[1] += fmaxf(-Fs, 0.0f); }
+            if (N.kind[N.fr[f]] >= 2) { bsum[0] += fmaxf(-Fs, 0.0f); bsum[1] += fmaxf(Fs, 0.0f); }
+        }
+        __syncthreads();
+        // update in float64, clip, semi-implicit friction; ghosts keep their filled state
+        // (swe1d.py:345-368)
+        for (int i = tid; i < nc; i += nt) {
+            float dA = 0.0f, dQ = 0.0f;
+            for (int j = N.lstart[i]; j < N.lstart[i + 1]; ++j) { const int f = N.lidx[j]; dA -= F1[f]; dQ -= F2[f] - pL[f]; }
+            for (int j = N.rstart[i]; j < N.rstart[i + 1]; ++j) { const int f = N.ridx[j]; dA += F1[f]; dQ += F2[f] - pR[f]; }
+            const int kd = N.kind[i];
+            const float rdx = 1.0f / N.dxf[i];
+            double A1 = Ag[i] + (double)(dt * dA * rdx);
+            double Q1 = Qg[i] + (double)(dt * dQ * rdx);
+            const double neg = clamp0(-A1);
+            bsum[2] += neg * N.dx[i] * (kd >= 2 ? 0.0 : 1.0);
+            A1 = A1 + neg;
+            const float A1f = (float)A1;
+            const float y1 = secf_depth(s, i, A1f);
+            const float Ac = fmaxf(A1f, 1e-12f);
+            const float R = Ac / secf_perim(s, i, y1);
+            const float nm = N.nmanf[i];
+            const float denom = 1.0f + dt * g * (nm * nm) * fabsf((float)Q1) / (Ac * powf(fmaxf(R, h_dry), 4.0f / 3.0f));
+            Q1 = Q1 / (double)denom;
+            if (!((y1 >= h_dry) && kd != 1)) Q1 = 0.0;
+            if (kd >= 2) { A1 = Ag[i]; Q1 = Qg[i]; }
+            A[i] = A1;
+            Q[i] = Q1;
+        }
+        bsum[0] *= (double)dt;
+        bsum[1] *= (double)dt;
+        block_sum<3>(bsum, red);
+        if (tid == 0) {
+            tot_in += bsum[0];
+            tot_out += bsum[1];
+            tot_clip += bsum[2];
+        }
+    }
+    __syncthreads();
+    for (int i = tid; i < nc; i += nt) { N.A[i] = A[i]; N.Q[i] = Q[i]; }
+    if (snap_eta) {                         // output: level z + depth and discharge (coupling.py:229-242)
+        double v1 = 0.0;
+        for (int i = tid; i < nc; i += nt) {
+            snap_eta[i] = (float)(N.z[i] + sec_depth(sd, i, A[i]));
+            snap_q[i] = (float)Q[i];
+            if (N.kind[i] <= 1) v1 += A[i] * N.dx[i];
+        }
+        if (snap_v1d) {                     // channel volume over the interior cells (swe1d.py:245-247)
+            double vv[1] = {v1};
+            block_sum<1>(vv, red);
+            if (tid == 0) *snap_v1d = vv[0];
+        }
+    }
+    if (tid == 0 && vols) {
+        vols[0] = tot_in;
+        vols[1] = tot_out;
+        vols[2] = tot_clip;
+    }
+}
 
 __host__ __device__ inline size_t exchange_smem_bytes(int n_links, int n_unique, int n_cells) {
     const size_t f64 = sizeof(double) * (2 * (size_t)n_links + 2 * (size_t)n_unique + (size_t)n_cells + 32 * 2);
