@@ -88,6 +88,7 @@ SIGNATURES = {
     "his_grid_step": (C.c_int32, [_H, C.POINTER(StepParams), _F64P, C.c_void_p]),
     "his_grid_max_rate": (C.c_int32, [_H, _F64P, C.c_void_p]),
     "his_grid_step_async": (C.c_int32, [_H, C.POINTER(StepParams), C.c_void_p, C.c_void_p]),
+    "his_grid_step_ledger_async": (C.c_int32, [_H, C.POINTER(StepParams), C.c_void_p, C.c_void_p]),
     "his_grid_max_rate_async": (C.c_int32, [_H, C.c_void_p, C.c_void_p]),
     "his_grid_volumes": (C.c_int32, [_H, _F64P, C.c_void_p]),
     "his_grid_step_noalloc": (C.c_int32, [C.c_int32, C.POINTER(SolverCfg), C.POINTER(GridDesc),
@@ -97,6 +98,7 @@ SIGNATURES = {
     "his_net_step": (C.c_int32, [_H, C.c_double, C.c_int32, _F64P, _F64P, C.c_void_p]),
     "his_net_max_rate": (C.c_int32, [_H, _F64P, _I32P, C.c_void_p]),
     "his_net_step_async": (C.c_int32, [_H, C.c_double, C.c_int32, _F64P, C.c_void_p, C.c_void_p]),
+    "his_net_step_ledger_async": (C.c_int32, [_H, C.c_double, C.c_int32, _F64P, C.c_void_p, C.c_void_p]),
     "his_net_max_rate_async": (C.c_int32, [_H, C.c_void_p, C.c_void_p]),
     "his_net_volume": (C.c_int32, [_H, _F64P, C.c_void_p]),
     "his_links_create": (C.c_int32, [_H, _H, C.c_int32, C.POINTER(LinksDesc), C.POINTER(_H)]),

@@ -174,9 +174,9 @@ class CoupledEngine:
         # the 1-D substeps overlap the 2-D step (disjoint state once the exchange is done)
         self._side = torch.cuda.Stream(two.device) if one is not None else None
         self._exchanged = torch.cuda.Event() if one is not None else None
-        # volumes of the step in flight, added to the mass terms on the device
-        self._vol2d = torch.zeros((two.B, 5), dtype=torch.float64, device=two.device)
-        self._vol1d = torch.zeros((two.B, 3), dtype=torch.float64, device=two.device) if one is not None else None
+        # the step kernels add their volume terms straight into the mass balance's device
+        # ledger: no copy and no extra kernel per step
+        self._ledger = self.mb.device_ledger(two.device)
         # state version of the 1-D model when its rates were last reduced ahead (None: not)
         self._rates1_at = None
 
@@ -245,7 +245,8 @@ class CoupledEngine:
 
     def step(self, t: float, t_limit: float, dt: float | None = None, n_sub: int | None = None) -> float:
         """One coupled step (coupling.py:205-230): CFL dt and 1-D substep count, the
-        exchange, the 2-D step and the 1-D substeps, mass terms added on the device.
+        exchange, the 2-D step and the 1-D substeps, mass terms added on the device by
+        the step kernels themselves.
         The step waits on the GPU once, for the CFL rates; the 1-D substeps run on a
         side stream beside the 2-D step and join before the step returns."""
         two, one = self.two, self.one
@@ -265,20 +266,17 @@ class CoupledEngine:
                 n_sub = max(1, math.ceil(dt / one.dt_from_rate(r1, wet1) - 1e-9))
             exchange(one, two, self.links, dt, self.cfg, volumes=False)
             self._exchanged.record(main)
-        two.step_into(dt, t, rain_t, edges_t, self._vol2d.data_ptr(), main.cuda_stream)
+        two.step_ledger(dt, t, rain_t, edges_t, self._ledger.data_ptr(), main.cuda_stream)
         if one is not None:
             # after the 2-D launch, so the host prepares the substeps while it runs;
             # the next step's 1-D rates are reduced right behind them, beside the 2-D
             side = self._side
             side.wait_event(self._exchanged)
-            one.substeps_into(dt, t, n_sub, self._vol1d.data_ptr(), side.cuda_stream)
+            one.substeps_ledger(dt, t, n_sub, self._ledger.data_ptr(), side.cuda_stream)
             one.rates_async(self._rates[two.B:], side.cuda_stream)
             self._rates1_at = one.state_version()
-        mb = self.mb
-        mb.add_columns(StepVolumes.TERMS, self._vol2d)
         if one is not None:
             main.wait_stream(self._side)
-            mb.add_columns(Step1DVolumes.TERMS, self._vol1d)
             self.log.n_sub_max = max(self.log.n_sub_max, n_sub)
             self._last_n_sub = n_sub
         self.log.steps += 1

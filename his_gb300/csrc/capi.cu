@@ -336,6 +336,26 @@ int32_t his_grid_step_async(his_grid* g, const his_step_params* params, double* 
     return HIS_OK;
 }
 
+// The caller's ledger must be device memory (the finalize kernel adds into it).
+static int check_ledger(double* ledger) {
+    cudaPointerAttributes a{};
+    if (cudaPointerGetAttributes(&a, ledger) != cudaSuccess || a.type != cudaMemoryTypeDevice) {
+        cudaGetLastError();
+        return bad("ledger must be device memory");
+    }
+    return HIS_OK;
+}
+
+int32_t his_grid_step_ledger_async(his_grid* g, const his_step_params* params, double* ledger, void* stream) {
+    if (!g || !params || !ledger) return bad("grid, params and ledger are required");
+    int rc = check_ledger(ledger);
+    if (rc) return rc;
+    if (!g->n_parts && (rc = grid_parts_setup(g))) return rc;
+    cudaStream_t s = (cudaStream_t)stream;
+    if ((rc = upload_params_pinned(g, params, s))) return rc;
+    return g->prec == HIS_PREC_F64 ? grid_step_f64(g, s, nullptr, ledger) : grid_step_f32(g, s, nullptr, ledger);
+}
+
 int32_t his_grid_max_rate_async(his_grid* g, double* rate, void* stream) {
     if (!g || !rate) return bad("grid and rate are required");
     bool direct = false;
@@ -524,6 +544,24 @@ int32_t his_net_step_async(his_net* N, double dt, int32_t n_sub, const double* f
     if ((rc = net_step_launch(N, dt, n_sub, s, direct ? vols : nullptr)) || !vols || direct) return rc;
     HIS_CK(cudaMemcpyAsync(vols, N->d_out, sizeof(double) * 3 * N->n, cudaMemcpyDefault, s));
     return HIS_OK;
+}
+
+int32_t his_net_step_ledger_async(his_net* N, double dt, int32_t n_sub, const double* forcing, double* ledger,
+                                  void* stream) {
+    if (!N || !forcing || !ledger) return bad("network, forcing and ledger are required");
+    if (n_sub < 1 || n_sub > N->max_sub) return bad("n_sub must be in [1, 256]");
+    if (!std::isfinite(dt) || !(dt >= 0)) return bad("dt must be finite and >= 0");
+    int rc = check_ledger(ledger);
+    if (rc) return rc;
+    cudaStream_t s = (cudaStream_t)stream;
+    size_t bytes = sizeof(double) * 2 * n_sub * N->n;
+    int slot = 0;
+    void* pin = stage_acquire(N->forcing_stage, bytes, &slot);
+    if (!pin) return HIS_ERR_CUDA;
+    std::memcpy(pin, forcing, bytes);
+    HIS_CK(cudaMemcpyAsync(N->d_forcing, pin, bytes, cudaMemcpyHostToDevice, s));
+    if ((rc = stage_release(N->forcing_stage, slot, s))) return rc;
+    return net_step_launch(N, dt, n_sub, s, nullptr, ledger);
 }
 
 int32_t his_net_max_rate_async(his_net* N, double* rate_wet, void* stream) {

@@ -26,6 +26,11 @@ enum : int {
     NPART
 };
 
+// Rows of the coupled step's float64 volume ledger (8 x members, row-major), in the
+// reference's term order with the clip of each model in its own row, so that the 2-D
+// and 1-D kernels of a step, which run on two streams, never add to the same element
+enum : int { LG_RAIN = 0, LG_INFIL, LG_BND2_IN, LG_BND2_OUT, LG_BND1_IN, LG_BND1_OUT, LG_CLIP2, LG_CLIP1, LEDGER_ROWS };
+
 // Member status in the device-resident engine
 enum : int { ST_RUNNING = 0, ST_DONE = 1, ST_NONFINITE = 2, ST_IMPLAUSIBLE = 3, ST_SUBSTEPS = 4 };
 constexpr double MAX_PLAUSIBLE_DEPTH_2D = 10.0;   // coupling.py:39
@@ -291,6 +296,9 @@ __device__ __forceinline__ void discharge_ghost(const KC<R>& c, R val, R h, R& h
 
 template <class R>
 __device__ __forceinline__ R minmod(R a, R b) {
+    // float32: the same value from four min/max and an add (for finite a, b: the
+    // smaller magnitude with the common sign, zero when the signs differ)
+    if constexpr (sizeof(R) == 4) return fmaxf(fminf(a, b), 0.0f) + fminf(fmaxf(a, b), 0.0f);
     if (a * b > R(0)) {
         R m = rmin(fabs(a), fabs(b));
         return a > R(0) ? m : -m;

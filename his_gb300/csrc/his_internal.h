@@ -158,8 +158,9 @@ int grid_init_f32(his_grid* g);
 // ext: optional device-writable copy of the outputs (step: 5 volumes per member;
 // reduce: the rate per member), written by the finalize kernel itself; rate_only:
 // the CFL rate alone (d_out's volume columns are left as they were)
-int grid_step_f64(his_grid* g, cudaStream_t s, double* ext = nullptr);
-int grid_step_f32(his_grid* g, cudaStream_t s, double* ext = nullptr);
+// ledger: optional device 8 x n float64 ledger the step's volume terms are added into
+int grid_step_f64(his_grid* g, cudaStream_t s, double* ext = nullptr, double* ledger = nullptr);
+int grid_step_f32(his_grid* g, cudaStream_t s, double* ext = nullptr, double* ledger = nullptr);
 int grid_reduce_f64(his_grid* g, cudaStream_t s, double* ext = nullptr, bool rate_only = false);
 int grid_reduce_f32(his_grid* g, cudaStream_t s, double* ext = nullptr, bool rate_only = false);
 int exchange_f64(his_links* l, const Consts& c, double dt, cudaStream_t s);
@@ -176,7 +177,7 @@ int engine_profile_f32(his_engine* e, int n_steps, double* ms);
 
 // net1d.cu
 // vols / rate_wet: optional device-writable outputs (3 per member; rate and wet per member)
-int net_step_launch(his_net* n, double dt, int n_sub, cudaStream_t s, double* vols = nullptr);
+int net_step_launch(his_net* n, double dt, int n_sub, cudaStream_t s, double* vols = nullptr, double* ledger = nullptr);
 int net_reduce_launch(his_net* n, cudaStream_t s, double* rate_wet = nullptr);
 int net_engine_launch(his_engine* e, cudaStream_t s, int m0, int count);
 int net_engine_prepare(his_engine* e);

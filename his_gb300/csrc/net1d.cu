@@ -7,11 +7,25 @@ namespace his {
 
 // n_sub substeps of dt/n_sub each for every member; forcing: per member, per
 // substep (inflow, stage); vols: 3 per member.
+// ledger (optional): 8 x members float64 ledger; the substeps' boundary volumes and
+// clip are added into its 1-D rows.
 __global__ void net_step_kernel(const Net* __restrict__ nets, Consts c, double dt_total, int n_sub,
-                                const double* __restrict__ forcing, double* __restrict__ vols) {
+                                const double* __restrict__ forcing, double* __restrict__ vols,
+                                double* __restrict__ ledger) {
     extern __shared__ double sm[];
+    __shared__ double v[3];
     net_substeps_dev(nets[blockIdx.x], c, dt_total, n_sub, forcing + (size_t)blockIdx.x * n_sub * 2,
-                     vols ? vols + blockIdx.x * 3 : nullptr, sm);
+                     (vols || ledger) ? v : nullptr, sm);
+    if (threadIdx.x == 0) {
+        if (vols)
+            for (int j = 0; j < 3; ++j) vols[blockIdx.x * 3 + j] = v[j];
+        if (ledger) {
+            const size_t B = gridDim.x;
+            ledger[LG_BND1_IN * B + blockIdx.x] += v[0];
+            ledger[LG_BND1_OUT * B + blockIdx.x] += v[1];
+            ledger[LG_CLIP1 * B + blockIdx.x] += v[2];
+        }
+    }
 }
 
 // 1-D CFL rate over wet interior cells, the any-wet flag and the channel volume.
@@ -83,10 +97,11 @@ int net_engine_launch(his_engine* e, cudaStream_t s, int m0, int count) {
     return HIS_OK;
 }
 
-int net_step_launch(his_net* n, double dt, int n_sub, cudaStream_t s, double* vols) {
+int net_step_launch(his_net* n, double dt, int n_sub, cudaStream_t s, double* vols, double* ledger) {
     if (n->smem > 48 * 1024)
         HIS_CK(cudaFuncSetAttribute(net_step_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)n->smem));
-    net_step_kernel<<<n->n, 128, n->smem, s>>>(n->d_nets, n->c, dt, n_sub, n->d_forcing, vols ? vols : n->d_out);
+    net_step_kernel<<<n->n, 128, n->smem, s>>>(n->d_nets, n->c, dt, n_sub, n->d_forcing,
+                                               vols ? vols : (ledger ? nullptr : n->d_out), ledger);
     HIS_CK(cudaGetLastError());
     return HIS_OK;
 }

@@ -4,7 +4,9 @@
 
 namespace his {
 int grid_init_f32(his_grid* g) { return grid_init_impl<float>(g); }
-int grid_step_f32(his_grid* g, cudaStream_t s, double* ext) { return grid_step_impl<float>(g, s, ext); }
+int grid_step_f32(his_grid* g, cudaStream_t s, double* ext, double* ledger) {
+    return grid_step_impl<float>(g, s, ext, ledger);
+}
 int grid_reduce_f32(his_grid* g, cudaStream_t s, double* ext, bool rate_only) {
     return grid_reduce_impl<float>(g, s, ext, rate_only);
 }

@@ -4,7 +4,9 @@
 
 namespace his {
 int grid_init_f64(his_grid* g) { return grid_init_impl<double>(g); }
-int grid_step_f64(his_grid* g, cudaStream_t s, double* ext) { return grid_step_impl<double>(g, s, ext); }
+int grid_step_f64(his_grid* g, cudaStream_t s, double* ext, double* ledger) {
+    return grid_step_impl<double>(g, s, ext, ledger);
+}
 int grid_reduce_f64(his_grid* g, cudaStream_t s, double* ext, bool rate_only) {
     return grid_reduce_impl<double>(g, s, ext, rate_only);
 }

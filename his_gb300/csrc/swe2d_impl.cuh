@@ -63,11 +63,11 @@ int launch_stages_parted(his_grid* g, cudaStream_t s) {
 }
 
 template <class R, int NT>
-int launch_step_nt(his_grid* g, cudaStream_t s, double* ext) {
+int launch_step_nt(his_grid* g, cudaStream_t s, double* ext, double* ledger) {
     int rc = launch_stages_parted<R, NT>(g, s);
     if (rc) return rc;
     finalize_kernel<R><<<g->n, 32, 0, s>>>(reinterpret_cast<const Grid<R>*>(g->d_grids), g->d_params, g->c,
-                                           g->d_partials, g->d_out, 0, ext);
+                                           g->d_partials, g->d_out, 0, ext, ledger);
     HIS_CK(cudaGetLastError());
     return HIS_OK;
 }
@@ -171,8 +171,8 @@ int grid_init_impl(his_grid* g) {
 }
 
 template <class R>
-int grid_step_impl(his_grid* g, cudaStream_t s, double* ext) {
-    HIS_NT_DISPATCH(launch_step_nt, R, g, s, ext);
+int grid_step_impl(his_grid* g, cudaStream_t s, double* ext, double* ledger) {
+    HIS_NT_DISPATCH(launch_step_nt, R, g, s, ext, ledger);
 }
 
 template <class R>

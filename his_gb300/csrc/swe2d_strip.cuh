@@ -87,9 +87,11 @@ __device__ __forceinline__ HaloRaw<R> halo_fetch(const KC<R>& c, const Grid<R>& 
     const bool inx = (unsigned)gx < (unsigned)nx, iny = (unsigned)gy < (unsigned)ny;
     HaloRaw<R> a;
     if (!inx && !iny) { a.h = a.hu = a.hv = a.z = R(0); return a; }
-    size_t i;
+    // 32-bit cell indices (a grid holds at most 2^30 cells): one wide multiply-add forms
+    // each address
+    unsigned i;
     if (inx && iny) {
-        i = (size_t)gy * nx + gx;
+        i = (unsigned)gy * (unsigned)nx + (unsigned)gx;
     } else {
         const int ng = c.order == 1 ? 1 : 2;
         const bool alongx = !inx;
@@ -107,7 +109,7 @@ __device__ __forceinline__ HaloRaw<R> halo_fetch(const KC<R>& c, const Grid<R>& 
             layer = lo ? 0 : n - 1;
         }
         layer = layer < 0 ? 0 : (layer > n - 1 ? n - 1 : layer);
-        i = alongx ? (size_t)gy * nx + layer : (size_t)layer * nx + gx;
+        i = alongx ? (unsigned)gy * (unsigned)nx + (unsigned)layer : (unsigned)layer * (unsigned)nx + (unsigned)gx;
     }
     a.h = H[i];
     a.hu = HU[i];
@@ -153,7 +155,7 @@ struct CellIn {
 };
 
 template <class R, int STAGE>
-__device__ __forceinline__ CellIn<R> cell_fetch(const Grid<R>& gd, size_t i) {
+__device__ __forceinline__ CellIn<R> cell_fetch(const Grid<R>& gd, unsigned i) {
     CellIn<R> a;
     a.hu0 = gd.hu[i];
     a.hv0 = gd.hv[i];
@@ -300,7 +302,7 @@ struct StripPipe {
     // Raw values of an interior row at this thread's source column (its own column, or
     // the layer an x-ghost copies)
     __device__ __forceinline__ HaloRaw<R> fetch_in(int gy) const {
-        const size_t i = (size_t)gy * nx + scol;
+        const unsigned i = (unsigned)gy * (unsigned)nx + (unsigned)scol;
         return HaloRaw<R>{H[i], HU[i], HV[i], gd.z[i]};
     }
     // halo_build for a row inside the grid: an interior cell, or the x-ghost that the
@@ -335,17 +337,17 @@ struct StripPipe {
         }
         s_cell[k0 + ts] = c0;
         ra = FULL ? fetch_in(r + 1) : halo_fetch(c, gd, H, HU, HV, cx, r + 1);
-        if (upd) cin = cell_fetch<R, STAGE>(gd, (size_t)orow * nx + cxc);
+        if (upd) cin = cell_fetch<R, STAGE>(gd, (unsigned)orow * (unsigned)nx + (unsigned)cxc);
         R by0 = R(0), bx0 = R(0);
-        Q4<R> yf0{R(0), R(0), R(0), R(0)};
         const Q4<R> c2 = s_cell[k2 + ts];           // own cells of rows r-2 and r-1
-        if (FULL || r >= y0 - 1) {
-            const Q4<R> c1 = s_cell[k1 + ts];
-            // y-reconstruction of row r-1: normal velocity v, tangential u
+        const Q4<R> c1 = s_cell[k1 + ts];
+        // y-reconstruction of row r-1 (normal velocity v, tangential u); its face with
+        // row r-2 is formed in phase B beside the x-face, two independent chains
+        const bool yact = FULL || r >= y0 - 1;
+        Side<R> ylo = ylow, yum;
+        if (yact) {
             const Recon<R> yup = reconstruct(c, c2.a, c1.a, c0.a, c2.c, c1.c, c0.c, c2.b, c1.b, c0.b, c2.d, c1.d, c0.d);
-            const int fy = r - 1;
-            if (FULL || (r >= y0 && fy >= 0 && fy <= ny)) yf0 = side_flux(c, ylow, c2.d, c2.a, side_minus(yup), c1.d, c1.a);
-            if (FULL || r >= y0) s_yf[k1 + ts] = yf0;
+            yum = side_minus(yup);
             ylow = side_plus(yup);
             if (c.order == 2) by0 = bed_term(c, yup);
         }
@@ -363,7 +365,13 @@ struct StripPipe {
             if (c.order == 2) bx0 = bed_term(c, xr);
         }
         __syncthreads();
-        // ---- B: x-face between columns cx-1 and cx of row r-2
+        // ---- B: y-face between rows r-2 and r-1; x-face between columns cx-1 and cx of row r-2
+        Q4<R> yf0{R(0), R(0), R(0), R(0)};
+        if (yact) {
+            const int fy = r - 1;
+            if (FULL || (r >= y0 && fy >= 0 && fy <= ny)) yf0 = side_flux(c, ylo, c2.d, c2.a, yum, c1.d, c1.a);
+            if (FULL || r >= y0) s_yf[k1 + ts] = yf0;
+        }
         Q4<R> xf0{R(0), R(0), R(0), R(0)};
         if (xact) {
             const Q4<R> lp = s_rp[ts - 1];
@@ -424,7 +432,7 @@ struct StripPipe {
             if (orow == 0) { yin += relu(G1s); yout += relu(-G1s); }
             if (orow == ny - 1) { yin += relu(-G1n); yout += relu(G1n); }
         }
-        const size_t i = (size_t)orow * nx + cx;
+        const unsigned i = (unsigned)orow * (unsigned)nx + (unsigned)cx;
         R hn, hun, hvn;
         if (STAGE == 2) {
             hn = R(0.5) * (cin.h0 + h3 + dt * dh);
@@ -628,6 +636,8 @@ __global__ void __launch_bounds__(NT, StripGeom<R, NT>::min_ctas(STAGE)) strip_k
     const int r_lo = max(y0 + 3, 4), r_hi = min(y1 + 2, ny - 2);
     int r = y0 - 3;
     for (; r <= y1 + 2 && r < r_lo; ++r) pp.template row<false>(r);
+    // (not unrolled: four copies of the row body ran 1.75x slower, the hot loop no
+    // longer fitting the instruction cache beside the other member chains' kernels)
     for (; r <= r_hi; ++r) pp.template row<true>(r);
     for (; r <= y1 + 2; ++r) pp.template row<false>(r);
     __syncthreads();
@@ -731,11 +741,13 @@ __global__ void __launch_bounds__(NT) strip_rate_kernel(const Grid<R>* __restric
 // member = bnd_in, bnd_out, rain, infil, clip (m^3), rate (1/s), surface and retained
 // volume.  mode 0: after a step; mode 1: rate and volumes only; mode 2: rate only
 // (after strip_rate_kernel).  ext (optional, device-writable): mode 0 the 5 volumes,
-// modes 1 and 2 the rate, per member.
+// modes 1 and 2 the rate, per member.  ledger (optional, mode 0): an 8 x n_members
+// float64 ledger (rows LG_*) the step's rain, infiltration, boundary and clip volumes
+// are added into.
 template <class R>
 __global__ void finalize_kernel(const Grid<R>* __restrict__ grids, const StepParams* __restrict__ params, Consts c,
                                 const double* __restrict__ partials, double* __restrict__ out, int mode,
-                                double* __restrict__ ext) {
+                                double* __restrict__ ext, double* __restrict__ ledger = nullptr) {
     const int m = blockIdx.x, lane = threadIdx.x;
     const Grid<R>& gd = grids[m];
     if (mode == 0 && !params[m].active) return;
@@ -789,6 +801,14 @@ __global__ void finalize_kernel(const Grid<R>* __restrict__ grids, const StepPar
     if (ext) {
 #pragma unroll
         for (int j = 0; j < 5; ++j) ext[(size_t)m * 5 + j] = o[j];
+    }
+    if (ledger) {
+        const size_t B = gridDim.x;
+        ledger[LG_RAIN * B + m] += o[2];
+        ledger[LG_INFIL * B + m] += o[3];
+        ledger[LG_BND2_IN * B + m] += o[0];
+        ledger[LG_BND2_OUT * B + m] += o[1];
+        ledger[LG_CLIP2 * B + m] += o[4];
     }
 }
 

@@ -53,6 +53,7 @@ class MassBalance:
         self.v0 = v0
         self._n = self.batch or 1
         self._ledgers: dict[str, object] = {}     # device name -> (7, n) float64 tensor
+        self._device_ledgers: dict[str, object] = {}   # device name -> (8, n), filled by the library
         self._index_cache: dict = {}
         self.series: list[dict] = []
 
@@ -99,6 +100,18 @@ class MassBalance:
             raise ValueError(f"mass columns have shape {tuple(values.shape)}, expected ({self._n}, {len(names)})")
         self._ledger(values.device).index_add_(0, idx, values.t().to(torch.float64))
 
+    def device_ledger(self, device):
+        """An 8 x n float64 ledger on ``device`` that the library's step kernels add a
+        coupled step's volumes into (his_grid_step_ledger_async, his_net_step_ledger_async):
+        rows rain, infiltration, 2-D boundary in and out, 1-D boundary in and out, then
+        the 2-D and the 1-D clip.  It is read with the other accumulators."""
+        import torch
+        key = str(device)
+        led = self._device_ledgers.get(key)
+        if led is None:
+            led = self._device_ledgers[key] = torch.zeros((8, self._n), dtype=torch.float64, device=device)
+        return led
+
     def set_totals(self, totals: dict) -> None:
         """Replace the ledger by totals accumulated elsewhere (e.g. on the device)."""
         import torch
@@ -108,6 +121,8 @@ class MassBalance:
                 raise KeyError(name)
             led[_ROW[name]] = _host(v).reshape(self._n)
         self._ledgers = {"cpu": torch.as_tensor(led)}
+        for dev in self._device_ledgers.values():     # kept: the library holds their addresses
+            dev.zero_()
 
     # ---------------------------------------------------------------- reading
     def ledger(self) -> np.ndarray:
@@ -115,6 +130,11 @@ class MassBalance:
         total = np.zeros((len(TERMS), self._n))
         for led in self._ledgers.values():
             total += _host(led)
+        clip = _ROW["clip"]
+        for dev in self._device_ledgers.values():
+            d = _host(dev)
+            total[:clip] += d[:clip]
+            total[clip] += d[clip] + d[clip + 1]
         return total
 
     def sources(self) -> dict:

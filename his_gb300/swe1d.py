@@ -224,6 +224,19 @@ class SWE1D:
                                                     _lib.stream_handle() if stream is None else stream),
                        "his_net_step_async")
 
+    def substeps_ledger(self, dt: float, t: float, n_sub: int, ledger_ptr: int, stream: int | None = None) -> None:
+        """The substeps with their boundary volumes and clip added into an 8 x B float64
+        device ledger (``MassBalance.device_ledger``) on ``stream``."""
+        sub = dt / n_sub
+        f = self.forcing(t) if n_sub == 1 else np.stack([self.forcing(t + k * sub) for k in range(n_sub)], axis=1)
+        f = np.ascontiguousarray(f, dtype=np.float64)
+        self._kernel_writes += 1
+        with _lib.on_device(self.device):
+            _lib.check(self._lib.his_net_step_ledger_async(self._handle, float(dt), int(n_sub), _lib.as_p(f),
+                                                           ledger_ptr,
+                                                           _lib.stream_handle() if stream is None else stream),
+                       "his_net_step_ledger_async")
+
     def state_version(self) -> tuple:
         """Changes whenever A or Q is written: through torch (assignment, in-place ops)
         or by this library's substeps and exchange."""

@@ -261,6 +261,15 @@ class SWE2D:
                                                      _lib.stream_handle() if stream is None else stream),
                        "his_grid_step_async")
 
+    def step_ledger(self, dt: float, t: float, rain_rate, edges_t, ledger_ptr: int, stream: int | None = None) -> None:
+        """The step with its volume terms added into an 8 x B float64 device ledger
+        (``MassBalance.device_ledger``) by the step's own finalize kernel, on ``stream``."""
+        params = self.step_params(dt, t, rain_rate, edges_t)
+        with _lib.on_device(self.device):
+            _lib.check(self._lib.his_grid_step_ledger_async(self._handle, params, ledger_ptr,
+                                                            _lib.stream_handle() if stream is None else stream),
+                       "his_grid_step_ledger_async")
+
     def scratch_bytes(self) -> int:
         return int(self._lib.his_grid_scratch_bytes(self._handle))
 

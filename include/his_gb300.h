@@ -117,6 +117,15 @@ int32_t his_grid_max_rate(his_grid* grid, double* rate, void* stream);
  * device tensors. */
 int32_t his_grid_step_async(his_grid* grid, const his_step_params* params, double* vols, void* stream);
 
+/* One 2-D step of every member (his_grid_step_async's arguments and asynchrony) that
+ * adds its volume terms into a caller's DEVICE ledger instead of returning them:
+ * float64, 8 x n_members, row-major, rows rain, infiltration, 2-D boundary in, 2-D
+ * boundary out, 1-D boundary in, 1-D boundary out, 2-D clip, 1-D clip (this call adds
+ * to rows 0-3 and 6, from the step's own finalize kernel: no extra launch, no copy).
+ * Replaces the per-step MassBalance.add of rain, infil, bnd2d_in, bnd2d_out and clip
+ * after SWE2D.step (hydrointel/solver/coupling.py:213-218). */
+int32_t his_grid_step_ledger_async(his_grid* grid, const his_step_params* params, double* ledger, void* stream);
+
 /* his_grid_max_rate_async: as his_grid_max_rate into `rate` (n_members).
  * Replaces the reduction of hydrointel/solver/swe2d.py:179-193. */
 int32_t his_grid_max_rate_async(his_grid* grid, double* rate, void* stream);
@@ -183,6 +192,13 @@ int32_t his_net_max_rate(his_net* net, double* rate, int32_t* any_wet, void* str
  * hydrointel/solver/coupling.py:216-221, which adds device tensors. */
 int32_t his_net_step_async(his_net* net, double dt, int32_t n_sub, const double* forcing, double* vols,
                            void* stream);
+
+/* n_sub 1-D substeps (his_net_step_async's arguments and asynchrony) adding their
+ * boundary volumes and clip into rows 4, 5 and 7 of the DEVICE ledger described at
+ * his_grid_step_ledger_async.  Replaces the per-substep MassBalance.add of bnd1d_in,
+ * bnd1d_out and clip (hydrointel/solver/coupling.py:219-224). */
+int32_t his_net_step_ledger_async(his_net* net, double dt, int32_t n_sub, const double* forcing, double* ledger,
+                                  void* stream);
 
 /* his_net_max_rate_async: per member (rate, wet) into rate_wet (n_members x 2; wet is
  * 1.0 when any interior cell is wet, else 0.0).  Replaces the reductions of

@@ -49,3 +49,18 @@ def test_error_measure_and_failure_names_the_member():
     single = MassBalance("cpu", 50.0)
     single.add("rain", 5.0)
     assert single.check(55.0, 0.0) == 0.0
+
+
+def test_device_ledger_rows_read_as_the_reference_terms():
+    """The 8-row ledger the library's step kernels add into reads back as the seven
+    terms, the two models' clips summed, together with terms added from the host."""
+    mb = MassBalance("cpu", np.array([0.0, 0.0]))
+    led = mb.device_ledger("cpu")
+    assert tuple(led.shape) == (8, 2)
+    led += torch.arange(16, dtype=torch.float64).reshape(8, 2)
+    mb.add("rain", torch.tensor([1.0, 1.0], dtype=torch.float64))
+    s = mb.sources()
+    assert list(s["rain"]) == [1.0, 2.0] and list(s["bnd1d_out"]) == [10.0, 11.0]
+    assert list(s["clip"]) == [12.0 + 14.0, 13.0 + 15.0]
+    mb.set_totals({k: np.zeros(2) for k in TERMS})
+    assert mb.device_ledger("cpu") is led and float(led.abs().sum()) == 0.0
