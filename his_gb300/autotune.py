@@ -223,4 +223,73 @@ def choose_tile(device: torch.device, prec: int, cfg, descs, states: list[list[t
         return tile
 
 
-__all__ = ["choose_tile", "candidates", "tune_key", "cache_path", "tiles_per_member", "chain_bounds"]
+ENGINE_CANDIDATES_X = (58, 122)   # wider strips were never the fastest for the engine
+ENGINE_STEPS = 32                  # timed engine steps per candidate and round (two captured graphs)
+
+
+def choose_tile_engine(storms, cfg, precision: str, device: torch.device, couple: bool = True,
+                       use_cache: bool = True) -> tuple[int, int]:
+    """Fastest (tile_x, tile_y) for a device-resident engine over ``storms``, timed as
+    the engine itself runs: for every distinct decomposition an engine is built over
+    one throw-away copy of the members (state, fields and network), in that
+    decomposition's default member chains, and the advance of ENGINE_STEPS captured
+    steps is timed with CUDA events, best of ROUNDS interleaved rounds.  Timing the
+    grid step alone (``choose_tile``) misses how each chain's per-step kernels and
+    the side-stream network interleave with the 2-D stages, and ranked the
+    decompositions differently.  Cached like ``choose_tile`` under its own key."""
+    from .engine import FloodEngine, Member
+    dtype = torch.float64 if precision == "fp64" else torch.float32
+    prec = _lib.PREC_F64 if precision == "fp64" else _lib.PREC_F32
+    shapes = [(int(s.terrain.ny), int(s.terrain.nx)) for s in storms]
+    key = tune_key(device, prec, int(cfg.spatial_order), shapes) + f"|engine|coupled{int(bool(couple))}"
+    with _LOCK:
+        if use_cache:
+            if key in _MEM:
+                return _MEM[key]
+            hit = _load_file().get(key)
+            if hit:
+                _MEM[key] = tuple(hit["tile"])
+                return _MEM[key]
+    cands = [t for t in candidates(shapes) if t[0] in ENGINE_CANDIDATES_X]
+    zcache: dict = {}
+    members = [Member(s, dtype, device, couple, False, zcache) for s in storms]
+    stream = torch.cuda.current_stream(device)
+    best = {tile: float("inf") for tile in cands}
+    engines = {}
+    try:
+        for tile in cands:
+            fe = FloodEngine(members, cfg, precision, device, tile=tile, graph_steps=16)
+            fe.prepare(ENGINE_STEPS)
+            engines[tile] = fe
+        # warm up on the first candidate until the clocks have settled
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        first = engines[cands[0]]
+        e0.record(stream)
+        first.advance(ENGINE_STEPS)
+        e1.record(stream)
+        e1.synchronize()
+        per = max(e0.elapsed_time(e1) / ENGINE_STEPS, 1e-3)
+        first.advance(max(ENGINE_STEPS, int(WARMUP_MS / per) // 16 * 16))
+        for _ in range(ROUNDS):
+            for tile in cands:
+                e0.record(stream)
+                engines[tile].advance(ENGINE_STEPS)
+                e1.record(stream)
+                e1.synchronize()
+                best[tile] = min(best[tile], e0.elapsed_time(e1) / ENGINE_STEPS)
+    finally:
+        torch.cuda.synchronize(device)
+        for fe in engines.values():
+            fe.close()
+        del members
+    times = {f"{tx}x{ty}": ms for (tx, ty), ms in best.items()}
+    tile = tuple(int(v) for v in min(times, key=times.get).split("x"))
+    with _LOCK:
+        _MEM[key] = tile
+        if use_cache:
+            _store_file(key, tile, times)
+    return tile
+
+
+__all__ = ["choose_tile", "choose_tile_engine", "candidates", "tune_key", "cache_path", "tiles_per_member",
+           "chain_bounds"]

@@ -402,7 +402,7 @@ int32_t his_net_create(const his_solver_cfg* cfg, int32_t n_members, const his_n
     struct Offs { size_t kind, gsrc, fl, fr, gsign, ls, li, rs, ri, z, n, dx, b, m, yb, ts, fb, fm, fyb, fts;
                   size_t zf, dxf, bf, mf, ybf, tsf, nf, gsf, fbf, fmf, fybf, ftsf; };
     std::vector<Offs> offs(n_members);
-    size_t smem = 0;
+    size_t smem = 0, smem_f32 = 0;
     for (int mb = 0; mb < n_members; ++mb) {
         const his_net_desc& d = nets[mb];
         std::string who = "network " + std::to_string(mb) + ": ";
@@ -450,12 +450,15 @@ int32_t his_net_create(const his_solver_cfg* cfg, int32_t n_members, const his_n
         o.fbf = addf(d.fb, d.n_faces); o.fmf = addf(d.fm, d.n_faces); o.fybf = addf(d.fyb, d.n_faces);
         o.ftsf = addf(d.fts, d.n_faces);
         smem = std::max(smem, net_smem_bytes(d.n_cells, d.n_faces));
+        smem_f32 = std::max(smem_f32, net_smem_bytes_f32(d.n_cells, d.n_faces));
     }
-    if (smem > 200 * 1024) return bad("network too large for one thread block's shared memory");
+    if (smem > 200 * 1024 || smem_f32 > 200 * 1024)
+        return bad("network too large for one thread block's shared memory");
     his_net* N = new his_net();
     N->c = to_consts(cfg);
     N->n = n_members;
     N->smem = smem;
+    N->smem_f32 = smem_f32;
     N->max_sub = 256;
     cudaGetDevice(&N->device);
     auto fail = [&](cudaError_t e, const char* w) { int r = cuda_fail(e, w); his_net_destroy(N); return r; };

@@ -61,6 +61,7 @@ struct his_net {
     double* d_out = nullptr;                 // n x 3
     double* h_out = nullptr;
     size_t smem = 0;
+    size_t smem_f32 = 0;                     // the float32 substeps (staged geometry)
     HostStage forcing_stage;                 // his_net_step_async forcing
 };
 

@@ -20,15 +20,15 @@ __global__ void net_engine_kernel_f32(const Net* __restrict__ nets, Consts c, co
 }
 
 int net_engine_prepare_f32(his_engine* e) {
-    if (e->net && e->net->smem > 48 * 1024)
+    if (e->net && e->net->smem_f32 > 48 * 1024)
         HIS_CK(cudaFuncSetAttribute(net_engine_kernel_f32, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                    (int)e->net->smem));
+                                    (int)e->net->smem_f32));
     return HIS_OK;
 }
 
 int net_engine_launch_f32(his_engine* e, cudaStream_t s, int m0, int count) {
     his_net* n = e->net;
-    net_engine_kernel_f32<<<count, 128, n->smem, s>>>(n->d_nets, n->c, e->d_em, e->grid->d_params, e->d_netf,
+    net_engine_kernel_f32<<<count, 128, n->smem_f32, s>>>(n->d_nets, n->c, e->d_em, e->grid->d_params, e->d_netf,
                                                       e->max_sub, e->d_vol1d, m0);
     HIS_CK(cudaGetLastError());
     return HIS_OK;

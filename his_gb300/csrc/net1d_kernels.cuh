@@ -328,8 +328,15 @@ __device__ __forceinline__ void hll_1d_f32(float AL, float QL, float pL, float c
     F2o = F2;
 }
 
+// Shared memory of the float32 substeps: the state in float64 (A, Q and their
+// ghost-filled copies), a reduction slot, the per-substep float32 work arrays, and the
+// network's static geometry and connectivity staged once per launch, so that no phase
+// waits on a global load (a lone CTA per network has no other warps to hide it).
 __host__ __device__ inline size_t net_smem_bytes_f32(int n_cells, int n_faces) {
-    return sizeof(double) * (4 * (size_t)n_cells + 32 * 4) + sizeof(float) * (4 * (size_t)n_cells + 4 * (size_t)n_faces);
+    const size_t nc = (size_t)n_cells, nf = (size_t)n_faces;
+    return sizeof(double) * (4 * nc + 32 * 4) + sizeof(float) * (4 * nc + 4 * nf) +   // state, red; work
+           sizeof(float) * (8 * nc + 4 * nf) +                                       // cell and face geometry
+           sizeof(int) * (2 * nc + 2 * nf + 2 * (nc + 1) + 2 * nf) + 16;             // kinds, faces, CSR
 }
 
 // n_sub substeps of dt/n_sub each for the network N (the arguments of net_substeps_dev).
@@ -341,7 +348,25 @@ __device__ __forceinline__ void net_substeps_f32_dev(const Net& N, const Consts&
     double *A = sm, *Q = A + nc, *Ag = Q + nc, *Qg = Ag + nc, *red = Qg + nc;      // red: 128 doubles
     float *Af = reinterpret_cast<float*>(red + 32 * 4), *yv = Af + nc, *uv = yv + nc, *th = uv + nc;
     float *F1 = th + nc, *F2 = F1 + nf, *pL = F2 + nf, *pR = pL + nf;
-    const SecF s{N.bf, N.mf, N.ybf, N.tsf}, fs{N.fbf, N.fmf, N.fybf, N.ftsf};
+    // staged geometry
+    float *zs = pR + nf, *dxs = zs + nc, *bs = dxs + nc, *ms = bs + nc, *ybs = ms + nc, *tss = ybs + nc,
+          *nms = tss + nc, *gss = nms + nc;
+    float *fbs = gss + nc, *fms = fbs + nf, *fybs = fms + nf, *ftss = fybs + nf;
+    int *kind = reinterpret_cast<int*>(ftss + nf), *gsrc = kind + nc, *fl = gsrc + nc, *fr = fl + nf;
+    int *lst = fr + nf, *rst = lst + nc + 1, *lix = rst + nc + 1, *rix = lix + nf;
+    for (int i = tid; i < nc; i += nt) {
+        A[i] = N.A[i]; Q[i] = N.Q[i];
+        zs[i] = N.zf[i]; dxs[i] = N.dxf[i]; bs[i] = N.bf[i]; ms[i] = N.mf[i]; ybs[i] = N.ybf[i]; tss[i] = N.tsf[i];
+        nms[i] = N.nmanf[i]; gss[i] = N.gsignf[i];
+        kind[i] = N.kind[i]; gsrc[i] = N.gsrc[i];
+    }
+    for (int i = tid; i <= nc; i += nt) { lst[i] = N.lstart[i]; rst[i] = N.rstart[i]; }
+    for (int f = tid; f < nf; f += nt) {
+        fbs[f] = N.fbf[f]; fms[f] = N.fmf[f]; fybs[f] = N.fybf[f]; ftss[f] = N.ftsf[f];
+        fl[f] = N.fl[f]; fr[f] = N.fr[f];
+        lix[f] = N.lidx[f]; rix[f] = N.ridx[f];
+    }
+    const SecF s{bs, ms, ybs, tss}, fs{fbs, fms, fybs, ftss};
     const Sec sd{N.b, N.m, N.yb, N.ts};
     __shared__ float s_k[3];
     if (tid == 0) {
@@ -349,7 +374,6 @@ __device__ __forceinline__ void net_substeps_f32_dev(const Net& N, const Consts&
         s_k[1] = (float)c.h_dry;
         s_k[2] = (float)(dt_total / n_sub);
     }
-    for (int i = tid; i < nc; i += nt) { A[i] = N.A[i]; Q[i] = N.Q[i]; }
     __syncthreads();
     const float g = s_k[0], h_dry = s_k[1], dt = s_k[2];
     double tot_in = 0.0, tot_out = 0.0, tot_clip = 0.0;
@@ -358,21 +382,21 @@ __device__ __forceinline__ void net_substeps_f32_dev(const Net& N, const Consts&
         const float eta = (float)forcing[2 * k + 1];
         // ghost cells from the interior neighbour (swe1d.py:265-294)
         for (int i = tid; i < nc; i += nt) {
-            const int kd = N.kind[i];
+            const int kd = kind[i];
             if (kd < 2) {
                 Ag[i] = A[i];
                 Qg[i] = Q[i];
                 Af[i] = (float)A[i];
                 continue;
             }
-            const int src = N.gsrc[i];
-            const float As = (float)A[src], Qs = (float)Q[src], sg = N.gsignf[i];
+            const int src = gsrc[i];
+            const float As = (float)A[src], Qs = (float)Q[src], sg = gss[i];
             const float ys = secf_depth(s, i, As);
             const float un = sg * (ys >= h_dry ? Qs / fmaxf(As, 1e-12f) : 0.0f);
             const bool wet_i = ys >= h_dry;
             float An, Qn;
             if (kd == 3) {
-                const float yst = fmaxf(eta - N.zf[i], 0.0f);
+                const float yst = fmaxf(eta - zs[i], 0.0f);
                 float Ast = secf_area(s, i, yst);
                 const float ci = sqrtf(g * As / secf_top(s, i, ys));
                 const float cg = sqrtf(g * Ast / secf_top(s, i, yst));
@@ -382,7 +406,7 @@ __device__ __forceinline__ void net_substeps_f32_dev(const Net& N, const Consts&
                 An = Ast;
                 Qn = sg * Ast * un_st;
             } else if (kd == 2) {
-                const float b = N.bf[i];
+                const float b = bs[i];
                 const float yc = fmaxf(cbrtf(q_in * q_in / (g * b * b)), h_dry);
                 An = wet_i ? As : secf_area(s, i, yc);
                 Qn = -sg * q_in;
@@ -397,15 +421,15 @@ __device__ __forceinline__ void net_substeps_f32_dev(const Net& N, const Consts&
         __syncthreads();
         // depth and velocity; a junction's level-pool depth in float64
         for (int i = tid; i < nc; i += nt) {
-            const float y = N.kind[i] == 1 ? (float)sec_depth(sd, i, Ag[i]) : secf_depth(s, i, Af[i]);
+            const float y = kind[i] == 1 ? (float)sec_depth(sd, i, Ag[i]) : secf_depth(s, i, Af[i]);
             yv[i] = y;
             uv[i] = y >= h_dry ? (float)Qg[i] / fmaxf(Af[i], 1e-12f) : 0.0f;
         }
         __syncthreads();
         // face fluxes with hydrostatic reconstruction (swe1d.py:326-336)
         for (int f = tid; f < nf; f += nt) {
-            const int l = N.fl[f], r = N.fr[f];
-            const float zL = N.zf[l], zR = N.zf[r], zfc = fmaxf(zL, zR);
+            const int l = fl[f], r = fr[f];
+            const float zL = zs[l], zR = zs[r], zfc = fmaxf(zL, zR);
             const float yL = fmaxf(zL + yv[l] - zfc, 0.0f), yR = fmaxf(zR + yv[r] - zfc, 0.0f);
             const float AL = secf_area(fs, f, yL), AR = secf_area(fs, f, yR);
             const float uL = uv[l], uR = uv[r];
@@ -420,41 +444,41 @@ __device__ __forceinline__ void net_substeps_f32_dev(const Net& N, const Consts&
         // outflow limiter; ghosts unlimited (swe1d.py:337-344)
         for (int i = tid; i < nc; i += nt) {
             float out = 0.0f;
-            for (int j = N.lstart[i]; j < N.lstart[i + 1]; ++j) out += fmaxf(F1[N.lidx[j]], 0.0f);
-            for (int j = N.rstart[i]; j < N.rstart[i + 1]; ++j) out += fmaxf(-F1[N.ridx[j]], 0.0f);
-            const float vol = Af[i] * N.dxf[i];
+            for (int j = lst[i]; j < lst[i + 1]; ++j) out += fmaxf(F1[lix[j]], 0.0f);
+            for (int j = rst[i]; j < rst[i + 1]; ++j) out += fmaxf(-F1[rix[j]], 0.0f);
+            const float vol = Af[i] * dxs[i];
             const float need = out * dt;
             const float t = need > vol ? vol / (need > 0.0f ? need : 1.0f) : 1.0f;
-            th[i] = N.kind[i] >= 2 ? 1.0f : t;
+            th[i] = kind[i] >= 2 ? 1.0f : t;
         }
         __syncthreads();
         double bsum[3] = {0.0, 0.0, 0.0};
         for (int f = tid; f < nf; f += nt) {
-            const float sc = F1[f] > 0.0f ? th[N.fl[f]] : th[N.fr[f]];
+            const float sc = F1[f] > 0.0f ? th[fl[f]] : th[fr[f]];
             const float Fs = F1[f] * sc;
             F1[f] = Fs;
-            if (N.kind[N.fl[f]] >= 2) { bsum[0] += fmaxf(Fs, 0.0f); bsum[1] += fmaxf(-Fs, 0.0f); }
-            if (N.kind[N.fr[f]] >= 2) { bsum[0] += fmaxf(-Fs, 0.0f); bsum[1] += fmaxf(Fs, 0.0f); }
+            if (kind[fl[f]] >= 2) { bsum[0] += fmaxf(Fs, 0.0f); bsum[1] += fmaxf(-Fs, 0.0f); }
+            if (kind[fr[f]] >= 2) { bsum[0] += fmaxf(-Fs, 0.0f); bsum[1] += fmaxf(Fs, 0.0f); }
         }
         __syncthreads();
         // update in float64, clip, semi-implicit friction; ghosts keep their filled state
         // (swe1d.py:345-368)
         for (int i = tid; i < nc; i += nt) {
             float dA = 0.0f, dQ = 0.0f;
-            for (int j = N.lstart[i]; j < N.lstart[i + 1]; ++j) { const int f = N.lidx[j]; dA -= F1[f]; dQ -= F2[f] - pL[f]; }
-            for (int j = N.rstart[i]; j < N.rstart[i + 1]; ++j) { const int f = N.ridx[j]; dA += F1[f]; dQ += F2[f] - pR[f]; }
-            const int kd = N.kind[i];
-            const float rdx = 1.0f / N.dxf[i];
+            for (int j = lst[i]; j < lst[i + 1]; ++j) { const int f = lix[j]; dA -= F1[f]; dQ -= F2[f] - pL[f]; }
+            for (int j = rst[i]; j < rst[i + 1]; ++j) { const int f = rix[j]; dA += F1[f]; dQ += F2[f] - pR[f]; }
+            const int kd = kind[i];
+            const float rdx = 1.0f / dxs[i];
             double A1 = Ag[i] + (double)(dt * dA * rdx);
             double Q1 = Qg[i] + (double)(dt * dQ * rdx);
             const double neg = clamp0(-A1);
-            bsum[2] += neg * N.dx[i] * (kd >= 2 ? 0.0 : 1.0);
+            if (neg > 0.0 && kd < 2) bsum[2] += neg * N.dx[i];
             A1 = A1 + neg;
             const float A1f = (float)A1;
             const float y1 = secf_depth(s, i, A1f);
             const float Ac = fmaxf(A1f, 1e-12f);
             const float R = Ac / secf_perim(s, i, y1);
-            const float nm = N.nmanf[i];
+            const float nm = nms[i];
             const float denom = 1.0f + dt * g * (nm * nm) * fabsf((float)Q1) / (Ac * powf(fmaxf(R, h_dry), 4.0f / 3.0f));
             Q1 = Q1 / (double)denom;
             if (!((y1 >= h_dry) && kd != 1)) Q1 = 0.0;
@@ -478,7 +502,7 @@ __device__ __forceinline__ void net_substeps_f32_dev(const Net& N, const Consts&
         for (int i = tid; i < nc; i += nt) {
             snap_eta[i] = (float)(N.z[i] + sec_depth(sd, i, A[i]));
             snap_q[i] = (float)Q[i];
-            if (N.kind[i] <= 1) v1 += A[i] * N.dx[i];
+            if (kind[i] <= 1) v1 += A[i] * N.dx[i];
         }
         if (snap_v1d) {                     // channel volume over the interior cells (swe1d.py:245-247)
             double vv[1] = {v1};

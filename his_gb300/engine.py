@@ -314,8 +314,12 @@ class FloodEngine:
         if isinstance(tile, str):
             if tile != "auto":
                 raise ValueError(f"tile must be (tile_x, tile_y), None or 'auto' (got {tile!r})")
-            from .autotune import choose_tile
-            tile = choose_tile(self.device, self.prec, self.cfg, gdesc, [m.state() for m in members])
+            from .autotune import choose_tile, choose_tile_engine
+            if all(not isinstance(s, Member) for s in storms):
+                # new storms: time the candidates as this engine will run them
+                tile = choose_tile_engine(self.storms, self.cfg, precision, self.device, couple)
+            else:
+                tile = choose_tile(self.device, self.prec, self.cfg, gdesc, [m.state() for m in members])
         self.tile = tuple(tile) if tile is not None else (0, 0)
         tx, ty = self.tile
         with torch.cuda.device(self.device):
