@@ -37,12 +37,13 @@ class Links:
     cells), shared by every member, plus the device handle binding a grid set and a network."""
 
     def __init__(self, cell1d, zbank, length, z2, inv, uniq, one: SWE1D, two: SWE2D):
-        self.cell1d = torch.as_tensor(np.asarray(cell1d), dtype=torch.long)
-        self.zbank = torch.as_tensor(np.asarray(zbank, dtype=np.float64))
-        self.length = torch.as_tensor(np.asarray(length, dtype=np.float64))
-        self.z2 = torch.as_tensor(np.asarray(z2, dtype=np.float64))
-        self.inv = torch.as_tensor(np.asarray(inv), dtype=torch.long)
-        self.uniq_dev = torch.as_tensor(np.asarray(uniq), dtype=torch.long)
+        own = lambda a, dt=None: torch.from_numpy(np.array(a, dtype=dt))     # a private copy
+        self.cell1d = own(cell1d, np.int64)
+        self.zbank = own(zbank, np.float64)
+        self.length = own(length, np.float64)
+        self.z2 = own(z2, np.float64)
+        self.inv = own(inv, np.int64)
+        self.uniq_dev = own(uniq, np.int64)
         self.n_unique = int(len(self.uniq_dev))
         if one.B != two.B:
             raise ValueError(f"the 2-D model is batched {two.batch} and the 1-D model {one.batch}; they must match")

@@ -109,7 +109,7 @@ class Member:
         ter = storm.terrain
         ny, nx = ter.ny, ter.nx
         self.shape = (ny, nx)
-        T = lambda a: torch.as_tensor(np.ascontiguousarray(a), dtype=dtype, device=device)
+        T = lambda a: torch.as_tensor(np.array(a, order="C"), dtype=dtype, device=device)
         if zcache is not None and id(ter) in zcache:
             self.z = zcache[id(ter)]
         else:

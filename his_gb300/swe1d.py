@@ -3,8 +3,9 @@
 of ``libhis_gb300.so`` (one CTA per member, the whole network in shared memory).
 
 State ``A`` (wetted area) and ``Q`` (discharge), (n_cells,) or (B, n_cells), are
-float64 CUDA buffers in both precisions (the 1-D network and its level-pool
-junctions are float64 islands of the production form).
+float64 CUDA buffers, and this drop-in solver steps them in float64 whatever the
+2-D model's precision.  The device-resident engine's float32 form runs its networks'
+arithmetic in float32 with the same float64 state and junction depths.
 """
 from __future__ import annotations
 
@@ -34,38 +35,63 @@ class Step1DVolumes:
 
 @dataclass
 class Sections:
-    """Trapezoid with vertical walls above the bank (swe1d.py:50-84), torch form for
-    host-side queries (initial levels, output stages); the step uses the kernel's own."""
+    """Cross-section geometry of every 1-D cell (or face), torch form for host-side
+    queries (levels, depths, plausibility); the step evaluates the same closed forms
+    in the network kernel.
+
+    A section is a trapezoid of bottom width b and side slope m (horizontal per
+    vertical) up to the bankfull depth yb, continued above the bank by vertical walls
+    ts apart.  Its width at height s above the bed is w(s) = b + 2 m s for s <= yb and
+    ts above, and every quantity below is an integral of w over the wetted height y:
+    the area A = int_0^y w, the first moment of area about the surface
+    I1 = int_0^y (y - s) w(s) ds (the hydrostatic force per unit weight), the top
+    width T = w(y), and the wetted perimeter, which the vertical walls do not add to
+    (the channel above the bank is the floodplain's).  (hydrointel/solver/swe1d.py:51-84)"""
     b: torch.Tensor
     m: torch.Tensor
     yb: torch.Tensor
     ts: torch.Tensor
 
+    def _split(self, y):
+        """Depth in the trapezoid and height of water above the bank."""
+        return torch.minimum(y, self.yb), torch.clamp(y - self.yb, min=0.0)
+
+    def _trapezoid_area(self, yt):
+        # int_0^yt (b + 2 m s) ds
+        return yt * (self.b + self.m * yt)
+
     def bank_area(self):
-        return self.yb * (self.b + self.m * self.yb)
+        return self._trapezoid_area(self.yb)
 
     def area(self, y):
-        yt = torch.minimum(y, self.yb)
-        return yt * (self.b + self.m * yt) + self.ts * torch.clamp(y - self.yb, min=0.0)
+        yt, above = self._split(y)
+        return self._trapezoid_area(yt) + self.ts * above
 
     def top_width(self, y):
         return torch.where(y <= self.yb, self.b + 2.0 * self.m * y, self.ts)
 
     def i1(self, y):
-        yt = torch.minimum(y, self.yb)
-        above = torch.clamp(y - self.yb, min=0.0)
-        at = yt * (self.b + self.m * yt)
-        return self.b * yt * yt / 2.0 + self.m * yt ** 3 / 3.0 + at * above + self.ts * above * above / 2.0
+        yt, above = self._split(y)
+        # the trapezoid's own moment about its top, int_0^yt (yt - s)(b + 2 m s) ds
+        # = b yt^2 / 2 + m yt^3 / 3, then its whole area shifted down by the water
+        # standing above the bank, then the wall part's moment ts above^2 / 2
+        own = self.b * yt * yt / 2.0 + self.m * yt ** 3 / 3.0
+        return own + self._trapezoid_area(yt) * above + self.ts * above * above / 2.0
 
     def perimeter(self, y):
-        yt = torch.minimum(y, self.yb)
+        yt, _ = self._split(y)
+        # bed plus two sloping sides of length yt sqrt(1 + m^2)
         return self.b + 2.0 * yt * torch.sqrt(1.0 + self.m * self.m)
 
     def depth(self, A):
+        """Depth holding area A: below the bank the positive root of m y^2 + b y - A = 0,
+        written as 2 A / (b + sqrt(b^2 + 4 m A)) so that it stays exact as m -> 0 (a
+        rectangle, y = A / b) and has no cancellation; above the bank the extra area
+        spreads over the wall width ts."""
         A = torch.clamp(A, min=0.0)
-        ab = self.bank_area()
-        y_t = 2.0 * A / (self.b + torch.sqrt(self.b * self.b + 4.0 * self.m * A))
-        return torch.where(A <= ab, y_t, self.yb + (A - ab) / self.ts)
+        full = self.bank_area()
+        in_trapezoid = 2.0 * A / (self.b + torch.sqrt(self.b * self.b + 4.0 * self.m * A))
+        return torch.where(A <= full, in_trapezoid, self.yb + (A - full) / self.ts)
 
 
 class SWE1D:
