@@ -414,7 +414,7 @@ def workload_config(members: int) -> dict:
     """The workload both arms report: the batched production form on the seeded terrain."""
     return {"workload": f"batched uniform: {members} storms x 400x325 @ 20 m, coupled 1-D/2-D, per-member dt",
             "members": members, "cells_per_step": members * 400 * 325, "grid": "400x325", "dx_m": 20.0,
-            "precision": "fp32 state and fluxes, fp64 accumulators", "graph_steps": 16,
+            "precision": "fp32 2-D state and fluxes, fp32 1-D fluxes over fp64 1-D state, fp64 accumulators", "graph_steps": 16,
             "l2": "inputs larger than L2 (~0.5 GB touched per step), no flush"}
 
 
@@ -464,7 +464,7 @@ def run_ours(args, world, rank, local):
     traffic = read_traffic()
     out = {"metric": "cell-steps/s", "value": value, "unit": "cell-steps/s", "n_gpus": world, "steps": args.steps,
            "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True, "scaling": "weak",
-           "vs_baseline": None, "dtype": "f32 (f64 accumulators and 1-D network)",
+           "vs_baseline": None, "dtype": "f32 (f64 accumulators, 1-D channel state and junction depths)",
            "data": "synthetic (seeded terrain, forcing and networks)",
            "config": workload_config(members),
            "gpu_launches": LAUNCHES_PER_STEP * eng.chains * args.steps, "tile": list(eng.tile), "chains": eng.chains,
