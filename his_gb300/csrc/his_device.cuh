@@ -296,9 +296,9 @@ __device__ __forceinline__ void discharge_ghost(const KC<R>& c, R val, R h, R& h
 
 template <class R>
 __device__ __forceinline__ R minmod(R a, R b) {
-    // float32: the same value from four min/max and an add (for finite a, b: the
-    // smaller magnitude with the common sign, zero when the signs differ)
-    if constexpr (sizeof(R) == 4) return fmaxf(fminf(a, b), 0.0f) + fminf(fmaxf(a, b), 0.0f);
+    // float32: the median of (a, b, 0) from four min/max (for finite a, b: the smaller
+    // magnitude with the common sign, zero when the signs differ)
+    if constexpr (sizeof(R) == 4) return fmaxf(fminf(a, b), fminf(fmaxf(a, b), 0.0f));
     if (a * b > R(0)) {
         R m = rmin(fabs(a), fabs(b));
         return a > R(0) ? m : -m;

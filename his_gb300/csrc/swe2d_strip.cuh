@@ -154,8 +154,18 @@ struct CellIn {
     R h0, hu0, hv0, hu1, hv1, sf, ic, f0, fc, k, S, n, rw;
 };
 
+// Optional fields of a member, tested once per CTA: the row loop reads a bit of a
+// register instead of re-reading a 64-bit pointer from the shared record and
+// comparing it with null.
+enum : unsigned { FEAT_STORE = 1u, FEAT_HORTON = 2u, FEAT_RAINW = 4u, FEAT_PEAK = 8u, FEAT_PSPEED = 16u, FEAT_SNAP = 32u };
+template <class R>
+__device__ __forceinline__ unsigned grid_features(const Grid<R>& gd) {
+    return (gd.S ? FEAT_STORE : 0u) | (gd.f0 ? FEAT_HORTON : 0u) | (gd.rw ? FEAT_RAINW : 0u) |
+           (gd.pk ? FEAT_PEAK : 0u) | (gd.ps ? FEAT_PSPEED : 0u);
+}
+
 template <class R, int STAGE>
-__device__ __forceinline__ CellIn<R> cell_fetch(const Grid<R>& gd, unsigned i) {
+__device__ __forceinline__ CellIn<R> cell_fetch(const Grid<R>& gd, unsigned i, unsigned feat) {
     CellIn<R> a;
     a.hu0 = gd.hu[i];
     a.hv0 = gd.hv[i];
@@ -167,14 +177,15 @@ __device__ __forceinline__ CellIn<R> cell_fetch(const Grid<R>& gd, unsigned i) {
         a.h0 = a.hu1 = a.hv1 = R(0);
     }
     if (STAGE != 1) {
-        a.sf = gd.S ? gd.sf[i] : R(0);
-        a.S = gd.S ? gd.S[i] : R(0);
-        a.ic = gd.f0 ? gd.ic[i] : R(0);
-        a.f0 = gd.f0 ? gd.f0[i] : R(0);
-        a.fc = gd.f0 ? gd.fc[i] : R(0);
-        a.k = gd.f0 ? gd.k[i] : R(0);
+        const bool hs = feat & FEAT_STORE, hf = feat & FEAT_HORTON;
+        a.sf = hs ? gd.sf[i] : R(0);
+        a.S = hs ? gd.S[i] : R(0);
+        a.ic = hf ? gd.ic[i] : R(0);
+        a.f0 = hf ? gd.f0[i] : R(0);
+        a.fc = hf ? gd.fc[i] : R(0);
+        a.k = hf ? gd.k[i] : R(0);
         a.n = gd.n[i];
-        a.rw = gd.rw ? gd.rw[i] : R(0);
+        a.rw = (feat & FEAT_RAINW) ? gd.rw[i] : R(0);
     } else {
         a.sf = a.S = a.ic = a.f0 = a.fc = a.k = a.n = a.rw = R(0);
     }
@@ -290,6 +301,7 @@ struct StripPipe {
     const R* __restrict__ HU;
     const R* __restrict__ HV;
     int ts, cx, cxc, nx, ny, y0, y1, scol, xside, xkind;
+    unsigned feat;                     // FEAT_* bits of the member's optional fields
     bool col_in, do_out, west, east;
     R dt, rdx, rdy, idx, idy, rdt, tt;
     // carried state of this thread's column
@@ -337,7 +349,7 @@ struct StripPipe {
         }
         s_cell[k0 + ts] = c0;
         ra = FULL ? fetch_in(r + 1) : halo_fetch(c, gd, H, HU, HV, cx, r + 1);
-        if (upd) cin = cell_fetch<R, STAGE>(gd, (unsigned)orow * (unsigned)nx + (unsigned)cxc);
+        if (upd) cin = cell_fetch<R, STAGE>(gd, (unsigned)orow * (unsigned)nx + (unsigned)cxc, feat);
         R by0 = R(0), bx0 = R(0);
         const Q4<R> c2 = s_cell[k2 + ts];           // own cells of rows r-2 and r-1
         const Q4<R> c1 = s_cell[k1 + ts];
@@ -452,14 +464,14 @@ struct StripPipe {
         }
         // ---- rain, Horton infiltration, retention store (swe2d.py:330-360)
         R sf = cin.sf;
-        if (gd.rw) {
+        if (feat & FEAT_RAINW) {
             const R add = rdt * cin.rw;
             hn = hn + add;
             rainw += add;
         } else {
             hn = hn + rdt;
         }
-        if (gd.f0) {
+        if (feat & FEAT_HORTON) {
             const R rate_f = cin.fc + (cin.f0 - cin.fc) * rexp(-cin.k * tt);
             const R pot = rate_f * dt;
             const R take = rmin(pot, hn);
@@ -469,7 +481,7 @@ struct StripPipe {
             hun = hun * scale;
             hvn = hvn * scale;
             R taken = take;
-            if (gd.S) {
+            if (feat & FEAT_STORE) {
                 const R tks = rmin(pot - take, sf);
                 sf = sf - tks;
                 taken = taken + tks;
@@ -477,7 +489,7 @@ struct StripPipe {
             infil += taken;
             gd.ic[i] = cin.ic + taken;
         }
-        if (gd.S) {
+        if (feat & FEAT_STORE) {
             const R room = clamp0(cin.S - sf);
             const R fill = rmin(room, hn);
             const R safe = hn > R(0) ? hn : R(1);
@@ -513,7 +525,7 @@ struct StripPipe {
         } else {
             gd.h1[i] = hn; gd.hu1[i] = hun; gd.hv1[i] = hvn;
         }
-        if (gd.pk) gd.pk[i] = rmax(gd.pk[i], hn);
+        if (feat & FEAT_PEAK) gd.pk[i] = rmax(gd.pk[i], hn);
         // ---- CFL rate of the new state for the next step (swe2d.py:179-184)
         R u2, v2;
         if constexpr (sizeof(R) == 4) {
@@ -524,9 +536,9 @@ struct StripPipe {
         }
         // running peak speed and output use the KP velocities of the new state, as the
         // reference's snapshots do (swe2d.py:161-167, coupling.py:229-242)
-        if (gd.ps) gd.ps[i] = rmax(gd.ps[i], dsqrt(u2 * u2 + v2 * v2));
-        if (float* sh = s_snap[0]) {
-            sh[i] = (float)hn;
+        if (feat & FEAT_PSPEED) gd.ps[i] = rmax(gd.ps[i], dsqrt(u2 * u2 + v2 * v2));
+        if (feat & FEAT_SNAP) {
+            s_snap[0][i] = (float)hn;
             s_snap[1][i] = (float)u2;
             s_snap[2][i] = (float)v2;
         }
@@ -563,9 +575,13 @@ __device__ __forceinline__ int ghost_source_column(const KC<R>& c, const Grid<R>
 template <class R, int NT, int STAGE>
 __global__ void __launch_bounds__(NT, StripGeom<R, NT>::min_ctas(STAGE)) strip_kernel(const Grid<R>* __restrict__ grids,
                                                     const StripRef* __restrict__ strips,
-                                                    const StepParams* __restrict__ params, const KC<R> c,
+                                                    const StepParams* __restrict__ params, const KC<R> kc,
                                                     double* __restrict__ partials) {
     using G = StripGeom<R, NT>;
+    // the stages of the second-order method (1, 2) and the first-order step (0) are
+    // launched for their order only, so the order is a constant of the instantiation
+    KC<R> c = kc;
+    c.order = STAGE == 0 ? 1 : 2;
     constexpr int P = G::P;
     extern __shared__ __align__(32) unsigned char smem_raw[];
     __shared__ R bcv[4];
@@ -605,6 +621,7 @@ __global__ void __launch_bounds__(NT, StripGeom<R, NT>::min_ctas(STAGE)) strip_k
     const int cx = x0 - 3 + t;                        // this thread's column
     const int q = cx - x0;                            // column relative to the strip
     pp.ts = t + 1;
+    pp.feat = grid_features(gd) | (s_snap[0] ? FEAT_SNAP : 0u);      // FEAT_SNAP: outputs due this step
     pp.cx = cx;
     pp.cxc = cx < 0 ? 0 : (cx > nx - 1 ? nx - 1 : cx);
     pp.nx = nx;
