@@ -114,17 +114,20 @@ def links_from_cells(one: SWE1D, two: SWE2D, cell1d, cells2d, length) -> Links:
                  uniq, one, two)
 
 
-def exchange(one: SWE1D, two: SWE2D, links: Links, dt: float, cfg: SolverConfig, volumes: bool = True):
+def exchange(one: SWE1D, two: SWE2D, links: Links, dt: float, cfg: SolverConfig, volumes: bool = True,
+             stream: int | None = None):
     """Move water between the models in place; per-link volumes (m^3, + = 2-D -> 1-D)
-    as a float64 device tensor, enqueued on the current stream without waiting for it
-    (coupling.py:73-124).  ``volumes=False`` skips them (the coupled step discards them)."""
+    as a float64 device tensor, enqueued on ``stream`` (default: the current stream)
+    without waiting for it (coupling.py:73-124).  ``volumes=False`` skips them (the
+    coupled step discards them)."""
     V = torch.empty((links.B, links.n_links), dtype=torch.float64, device=two.device) if volumes else None
     cfgc = links.cfg_struct(cfg)
     one._kernel_writes += 1
     with _lib.on_device(two.device):
         _lib.check(links._lib.his_exchange_async(links._handle, C.byref(cfgc), float(dt),
                                                  V.data_ptr() if V is not None and V.numel() else None,
-                                                 _lib.stream_handle()), "his_exchange_async")
+                                                 _lib.stream_handle() if stream is None else stream),
+                   "his_exchange_async")
     if V is None:
         return None
     return V if one.batch is not None else V[0]
@@ -223,23 +226,23 @@ class CoupledEngine:
         v = v.cpu()
         return v if self.batch is not None else float(v)
 
-    def _enqueue_rates(self, need2: bool, need1: bool) -> None:
-        """Both CFL reductions of the current state, into one pinned buffer.  The 1-D
-        rates reduced ahead on the side stream at the end of the last step are the
-        current state's unless A or Q has been written since (state version)."""
+    def _enqueue_rates(self, need2: bool, need1: bool, stream: int) -> None:
+        """Both CFL reductions of the current state, into one pinned buffer, on
+        ``stream``.  The 1-D rates reduced ahead on the side stream at the end of the
+        last step are the current state's unless A or Q has been written since (state
+        version)."""
         B = self.two.B
         with _lib.on_device(self.two.device):
             if need2:
-                self.two.rates_async(self._rates[:B])
+                self.two.rates_async(self._rates[:B], stream)
             if need1 and self._rates1_at != self.one.state_version():
-                self.one.rates_async(self._rates[B:])
+                self.one.rates_async(self._rates[B:], stream)
         self._rates1_at = None
 
-    def _wait_rates(self):
-        """Largest 2-D rate and (largest 1-D rate, any wet), after one wait for the GPU."""
+    def _wait_rates(self, main):
+        """Largest 2-D rate and (largest 1-D rate, any wet), after one wait for ``main``."""
         B = self.two.B
-        with _lib.on_device(self.two.device):
-            torch.cuda.current_stream().synchronize()
+        main.synchronize()
         r = self._rates.numpy()
         rw = r[B:].reshape(B, 2)
         return float(r[:B].max()), float(rw[:, 0].max()), bool((rw[:, 1] > 0).any())
@@ -253,21 +256,22 @@ class CoupledEngine:
         two, one = self.two, self.one
         need1 = one is not None and n_sub is None
         wait = dt is None or need1
+        main = torch.cuda.current_stream(two.device)       # looked up once per step
+        ms = main.cuda_stream
         if wait:
-            self._enqueue_rates(dt is None, need1)
+            self._enqueue_rates(dt is None, need1, ms)
         # forcing at t does not depend on dt: evaluated while the GPU reduces
         rain_t = self.rain(t)
         edges_t = edge_values(two.bcs, t)
         if wait:
-            r2, r1, wet1 = self._wait_rates()
+            r2, r1, wet1 = self._wait_rates(main)
         dt = min(two.dt_from_rate(r2) if dt is None else dt, t_limit - t)
-        main = torch.cuda.current_stream(two.device)
         if one is not None:
             if n_sub is None:
                 n_sub = max(1, math.ceil(dt / one.dt_from_rate(r1, wet1) - 1e-9))
-            exchange(one, two, self.links, dt, self.cfg, volumes=False)
+            exchange(one, two, self.links, dt, self.cfg, volumes=False, stream=ms)
             self._exchanged.record(main)
-        two.step_ledger(dt, t, rain_t, edges_t, self._ledger.data_ptr(), main.cuda_stream)
+        two.step_ledger(dt, t, rain_t, edges_t, self._ledger.data_ptr(), ms)
         if one is not None:
             # after the 2-D launch, so the host prepares the substeps while it runs;
             # the next step's 1-D rates are reduced right behind them, beside the 2-D

@@ -215,6 +215,8 @@ int32_t his_grid_destroy(his_grid* g) {
         if (g->pev_join[k]) cudaEventDestroy(g->pev_join[k]);
     }
     if (g->pev_fork) cudaEventDestroy(g->pev_fork);
+    if (g->ledger_exec) cudaGraphExecDestroy(g->ledger_exec);
+    if (g->cap_stream) cudaStreamDestroy(g->cap_stream);
     delete g;
     return HIS_OK;
 }
@@ -346,14 +348,50 @@ static int check_ledger(double* ledger) {
     return HIS_OK;
 }
 
+// The ledger step's launches (stages of every part, finalize) captured once per ledger:
+// the same kernels with the same arguments every step (the step parameters are read
+// from the grid's device buffer, uploaded before the graph runs).
+static int capture_ledger_step(his_grid* g, double* ledger) {
+    if (!g->cap_stream) HIS_CK(cudaStreamCreateWithFlags(&g->cap_stream, cudaStreamNonBlocking));
+    if (g->ledger_exec) {
+        HIS_CK(cudaGraphExecDestroy(g->ledger_exec));
+        g->ledger_exec = nullptr;
+        g->ledger_exec_for = nullptr;
+    }
+    HIS_CK(cudaStreamBeginCapture(g->cap_stream, cudaStreamCaptureModeThreadLocal));
+    const int rc = g->prec == HIS_PREC_F64 ? grid_step_f64(g, g->cap_stream, nullptr, ledger)
+                                           : grid_step_f32(g, g->cap_stream, nullptr, ledger);
+    cudaGraph_t graph = nullptr;
+    const cudaError_t e = cudaStreamEndCapture(g->cap_stream, &graph);
+    if (rc || e != cudaSuccess) {
+        if (graph) cudaGraphDestroy(graph);
+        return rc ? rc : cuda_fail(e, "cudaStreamEndCapture");
+    }
+    const cudaError_t ei = cudaGraphInstantiate(&g->ledger_exec, graph, 0);
+    cudaGraphDestroy(graph);
+    HIS_CK(ei);
+    g->ledger_exec_for = ledger;
+    return HIS_OK;
+}
+
 int32_t his_grid_step_ledger_async(his_grid* g, const his_step_params* params, double* ledger, void* stream) {
     if (!g || !params || !ledger) return bad("grid, params and ledger are required");
-    int rc = check_ledger(ledger);
-    if (rc) return rc;
+    int rc = HIS_OK;
+    if (ledger != g->ledger_checked) {
+        if ((rc = check_ledger(ledger))) return rc;
+        g->ledger_checked = ledger;
+    }
     if (!g->n_parts && (rc = grid_parts_setup(g))) return rc;
     cudaStream_t s = (cudaStream_t)stream;
     if ((rc = upload_params_pinned(g, params, s))) return rc;
-    return g->prec == HIS_PREC_F64 ? grid_step_f64(g, s, nullptr, ledger) : grid_step_f32(g, s, nullptr, ledger);
+    // a caller capturing its own graph gets the launches themselves
+    cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+    HIS_CK(cudaStreamIsCapturing(s, &cs));
+    if (cs != cudaStreamCaptureStatusNone)
+        return g->prec == HIS_PREC_F64 ? grid_step_f64(g, s, nullptr, ledger) : grid_step_f32(g, s, nullptr, ledger);
+    if (g->ledger_exec_for != ledger && (rc = capture_ledger_step(g, ledger))) return rc;
+    HIS_CK(cudaGraphLaunch(g->ledger_exec, s));
+    return HIS_OK;
 }
 
 int32_t his_grid_max_rate_async(his_grid* g, double* rate, void* stream) {
@@ -554,8 +592,11 @@ int32_t his_net_step_ledger_async(his_net* N, double dt, int32_t n_sub, const do
     if (!N || !forcing || !ledger) return bad("network, forcing and ledger are required");
     if (n_sub < 1 || n_sub > N->max_sub) return bad("n_sub must be in [1, 256]");
     if (!std::isfinite(dt) || !(dt >= 0)) return bad("dt must be finite and >= 0");
-    int rc = check_ledger(ledger);
-    if (rc) return rc;
+    int rc = HIS_OK;
+    if (ledger != N->ledger_checked) {
+        if ((rc = check_ledger(ledger))) return rc;
+        N->ledger_checked = ledger;
+    }
     cudaStream_t s = (cudaStream_t)stream;
     size_t bytes = sizeof(double) * 2 * n_sub * N->n;
     int slot = 0;

@@ -47,6 +47,13 @@ struct his_grid {
     int part_t[MAX_PARTS + 1] = {};
     cudaStream_t ps[MAX_PARTS - 1] = {};
     cudaEvent_t pev_fork = nullptr, pev_join[MAX_PARTS - 1] = {};
+    // his_grid_step_ledger_async: the stage launches (all parts, forked and joined)
+    // and the finalize as one graph, captured on cap_stream on the first call for a
+    // ledger and launched on the caller's stream after the parameter upload
+    cudaStream_t cap_stream = nullptr;
+    cudaGraphExec_t ledger_exec = nullptr;
+    double* ledger_exec_for = nullptr;      // the ledger ledger_exec adds into
+    double* ledger_checked = nullptr;       // the last ledger found to be device memory
 };
 
 struct his_net {
@@ -63,6 +70,7 @@ struct his_net {
     size_t smem = 0;
     size_t smem_f32 = 0;                     // the float32 substeps (staged geometry)
     HostStage forcing_stage;                 // his_net_step_async forcing
+    double* ledger_checked = nullptr;        // the last ledger found to be device memory
 };
 
 struct his_links {

@@ -209,11 +209,12 @@ class SWE2D:
                        "his_grid_max_rate")
         return out
 
-    def rates_async(self, out: torch.Tensor) -> None:
+    def rates_async(self, out: torch.Tensor, stream: int | None = None) -> None:
         """Enqueue the per-member CFL rates into ``out`` (B float64, device or pinned
-        host memory), valid once the current stream reaches this point."""
+        host memory), valid once ``stream`` (default: the current one) reaches this point."""
         with _lib.on_device(self.device):
-            _lib.check(self._lib.his_grid_max_rate_async(self._handle, out.data_ptr(), _lib.stream_handle()),
+            _lib.check(self._lib.his_grid_max_rate_async(self._handle, out.data_ptr(),
+                                                         _lib.stream_handle() if stream is None else stream),
                        "his_grid_max_rate_async")
 
     def max_dt(self) -> float:

@@ -123,7 +123,11 @@ int32_t his_grid_step_async(his_grid* grid, const his_step_params* params, doubl
  * boundary out, 1-D boundary in, 1-D boundary out, 2-D clip, 1-D clip (this call adds
  * to rows 0-3 and 6, from the step's own finalize kernel: no extra launch, no copy).
  * Replaces the per-step MassBalance.add of rain, infil, bnd2d_in, bnd2d_out and clip
- * after SWE2D.step (hydrointel/solver/coupling.py:213-218). */
+ * after SWE2D.step (hydrointel/solver/coupling.py:213-218).
+ * The first call for a ledger captures the step's kernel launches as a CUDA graph on a
+ * library stream; later calls upload the parameters and launch that graph on `stream`
+ * (the same kernels and results).  On a stream that is capturing the caller's own
+ * graph the launches are issued one by one. */
 int32_t his_grid_step_ledger_async(his_grid* grid, const his_step_params* params, double* ledger, void* stream);
 
 /* his_grid_max_rate_async: as his_grid_max_rate into `rate` (n_members).
