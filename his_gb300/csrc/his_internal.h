@@ -174,7 +174,6 @@ int grid_reduce_f64(his_grid* g, cudaStream_t s, double* ext = nullptr, bool rat
 int grid_reduce_f32(his_grid* g, cudaStream_t s, double* ext = nullptr, bool rate_only = false);
 int exchange_f64(his_links* l, const Consts& c, double dt, cudaStream_t s);
 int exchange_f32(his_links* l, const Consts& c, double dt, cudaStream_t s);
-size_t stage_smem_bytes(int prec, int tx, int ty);
 
 // n_steps engine steps of chain `chain` on its own streams
 int engine_enqueue_f64(his_engine* e, int chain, int n_steps);

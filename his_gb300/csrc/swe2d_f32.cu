@@ -11,11 +11,6 @@ int grid_reduce_f32(his_grid* g, cudaStream_t s, double* ext, bool rate_only) {
     return grid_reduce_impl<float>(g, s, ext, rate_only);
 }
 int exchange_f32(his_links* l, const Consts& c, double dt, cudaStream_t s) { return exchange_impl<float>(l, c, dt, s); }
-size_t stage_smem_bytes(int prec, int tx, int ty) {
-    (void)ty;
-    const int nt = strip_threads(tx);
-    return prec == HIS_PREC_F64 ? stage_smem_impl<double>(nt) : stage_smem_impl<float>(nt);
-}
 int engine_enqueue_f32(his_engine* e, int chain, int n) { return engine_enqueue_impl<float>(e, chain, n); }
 int engine_take_rate_f32(his_engine* e) { return engine_take_rate_impl<float>(e); }
 int engine_profile_f32(his_engine* e, int n, double* ms) { return engine_profile_impl<float>(e, n, ms); }

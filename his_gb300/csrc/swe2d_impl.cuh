@@ -191,15 +191,6 @@ int exchange_impl(his_links* l, const Consts& c, double dt, cudaStream_t s) {
     return HIS_OK;
 }
 
-template <class R>
-size_t stage_smem_impl(int nt) {
-    if (nt == 64) return StripGeom<R, 64>::smem_bytes;
-    if (nt == 128) return StripGeom<R, 128>::smem_bytes;
-    if (nt == 224) return StripGeom<R, 224>::smem_bytes;
-    if (nt == 352) return StripGeom<R, 352>::smem_bytes;
-    return 0;
-}
-
 // One device-resident step for every member of one chain (see engine_kernels.cuh)
 // on the chain's main stream; the 1-D substeps run on its side stream between a
 // fork and a join event, concurrently with the 2-D stages.
