@@ -116,8 +116,8 @@ def peaks():
 class ClockSampler:
     """SM clocks and throttle reasons sampled during the timed region.
 
-    NVML (the driver's libnvidia-ml, read-only queries) is polled every millisecond
-    from a host thread, so even a timed region of a few milliseconds gets several
+    NVML (the driver's libnvidia-ml, read-only queries) is polled every 0.2 ms from a
+    host thread, so even a timed region of a few milliseconds gets a few dozen
     samples; without NVML, nvidia-smi every 200 ms."""
 
     REASONS = {0x4: "sw_power_cap", 0x8: "hw_slowdown", 0x20: "sw_thermal_slowdown", 0x40: "hw_thermal_slowdown"}
@@ -125,7 +125,7 @@ class ClockSampler:
               "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
               "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
 
-    def __init__(self, gpu_index: int, period_s: float = 0.001):
+    def __init__(self, gpu_index: int, period_s: float = 0.0002):
         self.gpu = gpu_index
         self.period = period_s
         self.samples = []            # (sm_mhz, reason bits)
@@ -178,7 +178,7 @@ class ClockSampler:
         except Exception:
             self._nvml = None
         if self._nvml is not None:
-            self.source = "nvml, 1 ms"
+            self.source = f"nvml, {self.period * 1e3:g} ms"
             self._stop = threading.Event()
             self._thread = threading.Thread(target=self._poll, daemon=True)
             self._thread.start()
