@@ -37,7 +37,7 @@ def arrival_times(depth_series, times, threshold: float = 0.1) -> np.ndarray:
 
 # The reference's own acceptance criteria for a float32 run against float64
 # (hydrointel/benchmarks/precision.py:37-44 and criteria.py:40-46); reported beside
-# the comparison, the benchmark spec's bar being peak-depth RMSE <= 1 cm.
+# the comparison; the production form's own bar is peak-depth RMSE <= 1 cm.
 REFERENCE_FP32_CRITERIA = {
     "mass_balance_error": 1e-4,
     "depth_max_abs_m": 5e-3,
@@ -169,7 +169,7 @@ def against_fp64(storms, interval_s: float, cfg=None, chunk: int = 1024, timeout
 
 def reference_criteria(m: dict) -> dict:
     """Each of the reference's float32 acceptance criteria with its value in ``m`` and
-    whether it holds (mass balance judged on the float32 run)."""
+    whether it holds (mass balance taken from the float32 run)."""
     vals = dict(m)
     vals.setdefault("mass_balance_error", m.get("mass_error_fp32"))
     return {k: {"value": vals.get(k), "limit": lim, "pass": vals.get(k) is not None and vals[k] <= lim}

@@ -28,7 +28,7 @@ extern "C" {
 #define HIS_ERR_WAIT_TIMEOUT 4   /* a bounded device wait gave up                                        */
 #define HIS_ERR_OOM_ADMISSION 5  /* request does not fit the HBM budget                                  */
 #define HIS_ERR_CUDA 6           /* CUDA runtime error (message via his_last_error)                      */
-#define HIS_ERR_UNSUPPORTED 7    /* feature not available in this build                                  */
+#define HIS_ERR_UNSUPPORTED 7    /* feature not available in this library                                */
 
 #define HIS_PREC_F64 0           /* plain method: all arithmetic float64                                  */
 #define HIS_PREC_F32 1           /* production form: float32 state and fluxes, float64 accumulators      */

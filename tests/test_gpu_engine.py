@@ -1,4 +1,4 @@
-"""The CUDA engine on the synthetic workloads: spec parity with the oracle, lake at
+"""The CUDA engine on the synthetic workloads: parity with the oracle at 1e-9, lake at
 rest, mass balance, per-member time steps, batched == solo, float32 production form."""
 import numpy as np
 import pytest
