@@ -117,8 +117,8 @@ class ClockSampler:
     """SM clocks and throttle reasons sampled during the timed region.
 
     NVML (the driver's libnvidia-ml, read-only queries) is polled every 0.2 ms from a
-    host thread, so even a timed region of a few milliseconds gets a few dozen
-    samples; without NVML, nvidia-smi every 200 ms."""
+    host thread (a read itself takes about 0.3 ms), so even a timed region of a few
+    milliseconds gets a dozen or more samples; without NVML, nvidia-smi every 200 ms."""
 
     REASONS = {0x4: "sw_power_cap", 0x8: "hw_slowdown", 0x20: "sw_thermal_slowdown", 0x40: "hw_thermal_slowdown"}
     FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
