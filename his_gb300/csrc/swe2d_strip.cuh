@@ -2,17 +2,17 @@
 //
 // A CTA of NT threads owns a strip of W <= NT - 6 columns of one member and marches
 // up a chunk of rows [y0, y1).  Thread t works on column cx = x0 - 3 + t.  Per new
-// row r it
-//   P1  loads row r of (h, u, v, z) into a ring of 8 rows (ghost cells built at the
-//       domain edges, boundaries.py:81-128),
-//   P2  computes the y-face between rows r-2 and r-1 (the lower cell's
-//       y-reconstruction is carried in registers from the previous row) and the
-//       x-reconstruction of row r-2,
-//   P3  computes the x-faces of row r-2,
-//   P4  computes the positivity-limiter theta of row r-2 (swe2d.py:259-264),
-//   P5  updates row r-3 (divergence of the donor-scaled fluxes, bed source, RK
-//       stage, then in the last stage rain, infiltration, retention, friction, CFL
-//       rate and peaks; swe2d.py:305-371).
+// row r, with two barriers (StripPipe::row below):
+//   A  builds row r of (h, u, v, z) into a four-row shared ring (ghost cells at the
+//      domain edges, boundaries.py:81-128), prefetches row r+1 and the update inputs
+//      of row r-3, forms the y-reconstruction of row r-1 and the x-reconstruction of
+//      row r-2 (swe2d.py:205-219) and publishes the latter's plus side;
+//   B  forms the y-face between rows r-2 and r-1 and the x-face west of its cell in
+//      row r-2 (swe2d.py:61-101, 226-234), two independent chains side by side;
+//   C  forms the positivity-limiter theta of row r-2 (swe2d.py:259-264);
+//   D  updates row r-3: divergence of the donor-scaled fluxes, bed source, RK stage,
+//      then in the last stage rain, infiltration, retention, friction, CFL rate and
+//      peaks (swe2d.py:305-371).
 // Every cell is loaded once (plus a 3-column halo each side) and every face flux,
 // reconstruction and theta is computed once.  Per-thread partial sums (clip,
 // boundary flux, infiltration, rain, rate, volumes) are reduced once per strip-chunk
