@@ -6,12 +6,15 @@
 // in the reference's index order, so every sum has the reference's association
 // and the result does not depend on thread scheduling.
 //
-// The 1-D network and its junction level pool are float64 in both precisions (a
-// float64 island of the production form).  The weir exchange is float64 in the
-// plain method; in the production form its per-link arithmetic is float32 (GB300's
-// float64 pipe runs at a small fraction of the float32 rate and this work sits on
-// every step's critical path), with the 1-D area update and the exchanged-volume
-// tallies kept in float64.
+// The drop-in 1-D step (net_step_kernel) is float64 in both precisions.  The
+// device-resident engine's float32 form (net_engine_kernel_f32) computes section
+// geometry, wave speeds, HLL fluxes, limiter and friction in float32 over float64
+// area and discharge state, float64 updates and tallies, and float64 junction depths
+// (the level-pool solve); its float64 form (net_engine_kernel) is float64 throughout.
+// The weir exchange is float64 in the plain method; in the production form its
+// per-link arithmetic is float32 (GB300's float64 pipe runs at a small fraction of the
+// float32 rate and this work sits on every step's critical path), with the 1-D area
+// update and the exchanged-volume tallies kept in float64.
 //
 // Reference: hydrointel/solver/swe1d.py:51-107, :253-368; coupling.py:73-124.
 #pragma once
