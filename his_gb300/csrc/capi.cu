@@ -384,12 +384,17 @@ int32_t his_grid_step_ledger_async(his_grid* g, const his_step_params* params, d
     if (!g->n_parts && (rc = grid_parts_setup(g))) return rc;
     cudaStream_t s = (cudaStream_t)stream;
     if ((rc = upload_params_pinned(g, params, s))) return rc;
-    // a caller capturing its own graph gets the launches themselves
+    // a caller capturing its own graph gets the launches themselves, and so does every
+    // step once a capture has failed (a capture the thread cannot open, for one)
     cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
     HIS_CK(cudaStreamIsCapturing(s, &cs));
-    if (cs != cudaStreamCaptureStatusNone)
+    if (cs == cudaStreamCaptureStatusNone && !g->ledger_graph_off && g->ledger_exec_for != ledger &&
+        capture_ledger_step(g, ledger) != HIS_OK) {
+        cudaGetLastError();
+        g->ledger_graph_off = true;
+    }
+    if (cs != cudaStreamCaptureStatusNone || g->ledger_graph_off)
         return g->prec == HIS_PREC_F64 ? grid_step_f64(g, s, nullptr, ledger) : grid_step_f32(g, s, nullptr, ledger);
-    if (g->ledger_exec_for != ledger && (rc = capture_ledger_step(g, ledger))) return rc;
     HIS_CK(cudaGraphLaunch(g->ledger_exec, s));
     return HIS_OK;
 }

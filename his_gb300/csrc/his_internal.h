@@ -54,6 +54,7 @@ struct his_grid {
     cudaGraphExec_t ledger_exec = nullptr;
     double* ledger_exec_for = nullptr;      // the ledger ledger_exec adds into
     double* ledger_checked = nullptr;       // the last ledger found to be device memory
+    bool ledger_graph_off = false;          // capture failed once: plain launches from then on
 };
 
 struct his_net {
