@@ -90,6 +90,7 @@ SIGNATURES = {
     "his_grid_step_async": (C.c_int32, [_H, C.POINTER(StepParams), C.c_void_p, C.c_void_p]),
     "his_grid_step_ledger_async": (C.c_int32, [_H, C.POINTER(StepParams), C.c_void_p, C.c_void_p]),
     "his_grid_max_rate_async": (C.c_int32, [_H, C.c_void_p, C.c_void_p]),
+    "his_grid_step_rate_async": (C.c_int32, [_H, C.c_void_p, C.c_void_p]),
     "his_grid_volumes": (C.c_int32, [_H, _F64P, C.c_void_p]),
     "his_grid_step_noalloc": (C.c_int32, [C.c_int32, C.POINTER(SolverCfg), C.POINTER(GridDesc),
                                           C.POINTER(StepParams), _F64P, C.c_void_p]),

@@ -123,6 +123,7 @@ def exchange(one: SWE1D, two: SWE2D, links: Links, dt: float, cfg: SolverConfig,
     V = torch.empty((links.B, links.n_links), dtype=torch.float64, device=two.device) if volumes else None
     cfgc = links.cfg_struct(cfg)
     one._kernel_writes += 1
+    two._kernel_writes += 1
     with _lib.on_device(two.device):
         _lib.check(links._lib.his_exchange_async(links._handle, C.byref(cfgc), float(dt),
                                                  V.data_ptr() if V is not None and V.numel() else None,
@@ -181,8 +182,10 @@ class CoupledEngine:
         # the step kernels add their volume terms straight into the mass balance's device
         # ledger: no copy and no extra kernel per step
         self._ledger = self.mb.device_ledger(two.device)
-        # state version of the 1-D model when its rates were last reduced ahead (None: not)
+        # state version of the 1-D model when its rates were last reduced ahead, and of
+        # the 2-D model when a step of this engine last left its rates (None: not)
         self._rates1_at = None
+        self._rates2_at = None
 
     def plausibility(self) -> np.ndarray:
         """Per member (rows): the largest 2-D depth and the highest 1-D water level above
@@ -227,14 +230,18 @@ class CoupledEngine:
         return v if self.batch is not None else float(v)
 
     def _enqueue_rates(self, need2: bool, need1: bool, stream: int) -> None:
-        """Both CFL reductions of the current state, into one pinned buffer, on
-        ``stream``.  The 1-D rates reduced ahead on the side stream at the end of the
-        last step are the current state's unless A or Q has been written since (state
-        version)."""
+        """Both CFL rates of the current state, into one pinned buffer, on ``stream``.
+        The 2-D rates are those the last step's own last stage formed, and the 1-D
+        rates those reduced ahead on the side stream at the end of the last step,
+        unless the state has been written since (state versions); then they are
+        reduced afresh."""
         B = self.two.B
         with _lib.on_device(self.two.device):
             if need2:
-                self.two.rates_async(self._rates[:B], stream)
+                if self._rates2_at is not None and self._rates2_at == self.two.state_version():
+                    self.two.step_rate_async(self._rates[:B], stream)
+                else:
+                    self.two.rates_async(self._rates[:B], stream)
             if need1 and self._rates1_at != self.one.state_version():
                 self.one.rates_async(self._rates[B:], stream)
         self._rates1_at = None
@@ -272,6 +279,7 @@ class CoupledEngine:
             exchange(one, two, self.links, dt, self.cfg, volumes=False, stream=ms)
             self._exchanged.record(main)
         two.step_ledger(dt, t, rain_t, edges_t, self._ledger.data_ptr(), ms)
+        self._rates2_at = two.state_version()        # its last stage formed the new state's rates
         if one is not None:
             # after the 2-D launch, so the host prepares the substeps while it runs;
             # the next step's 1-D rates are reduced right behind them, beside the 2-D

@@ -413,6 +413,16 @@ int32_t his_grid_max_rate_async(his_grid* g, double* rate, void* stream) {
     return HIS_OK;
 }
 
+int32_t his_grid_step_rate_async(his_grid* g, double* rate, void* stream) {
+    if (!g || !rate) return bad("grid and rate are required");
+    bool direct = false;
+    int rc = check_async_out(rate, "rate", &direct);
+    if (rc) return rc;
+    HIS_CK(cudaMemcpy2DAsync(rate, sizeof(double), g->d_out + 5, 8 * sizeof(double), sizeof(double), g->n,
+                             cudaMemcpyDefault, (cudaStream_t)stream));
+    return HIS_OK;
+}
+
 int32_t his_grid_max_rate(his_grid* g, double* rate, void* stream) {
     if (!g || !rate) return bad("grid and rate are required");
     cudaStream_t s = (cudaStream_t)stream;

@@ -115,6 +115,7 @@ class SWE2D:
         full = self.bshape + (self.ny, self.nx)
         zeros = torch.zeros(full, dtype=dtype, device=self.device)
         self._h, self._hu, self._hv = zeros.clone(), zeros.clone(), zeros.clone()
+        self._kernel_writes = 0          # the library's writes of h, hu, hv outside a step
         self._sf, self._ic = zeros.clone(), zeros.clone()
         self.n_dt_clamped = 0
         self._lib = _lib.load()
@@ -216,6 +217,20 @@ class SWE2D:
             _lib.check(self._lib.his_grid_max_rate_async(self._handle, out.data_ptr(),
                                                          _lib.stream_handle() if stream is None else stream),
                        "his_grid_max_rate_async")
+
+    def step_rate_async(self, out: torch.Tensor, stream: int | None = None) -> None:
+        """Enqueue the per-member CFL rates of the state the last step left into
+        ``out``, from that step's own last stage (no reduction); valid only while
+        ``state_version()`` is what it was after the step."""
+        with _lib.on_device(self.device):
+            _lib.check(self._lib.his_grid_step_rate_async(self._handle, out.data_ptr(),
+                                                          _lib.stream_handle() if stream is None else stream),
+                       "his_grid_step_rate_async")
+
+    def state_version(self) -> tuple:
+        """Changes whenever h, hu or hv is written: through torch (assignment, in-place
+        ops, set_state) or by this library outside a step (the weir exchange)."""
+        return (self._h._version, self._hu._version, self._hv._version, self._kernel_writes)
 
     def max_dt(self) -> float:
         """CFL step over the whole batch (the reference shares one dt across members)."""

@@ -134,6 +134,15 @@ int32_t his_grid_step_ledger_async(his_grid* grid, const his_step_params* params
  * Replaces the reduction of hydrointel/solver/swe2d.py:179-193. */
 int32_t his_grid_max_rate_async(his_grid* grid, double* rate, void* stream);
 
+/* The per-member CFL rate of the state the last step left, into `rate` (n_members,
+ * device or page-locked memory), without a reduction: the step's last stage forms
+ * each cell's rate from the values it stores (the same expression as the reduction)
+ * and its finalize keeps the maximum.  Valid only while the state is the last step's
+ * output: the caller tracks writes in between (then his_grid_max_rate_async).
+ * Replaces the reduction of hydrointel/solver/swe2d.py:179-193 at the start of a
+ * coupled step (coupling.py:205-207). */
+int32_t his_grid_step_rate_async(his_grid* grid, double* rate, void* stream);
+
 /* Per-member surface and retained volumes sum(h)*area, sum(s_filled)*area (host out,
  * n_members x 2; synchronises).  Replaces hydrointel/solver/swe2d.py:169-174. */
 int32_t his_grid_volumes(his_grid* grid, double* vols, void* stream);

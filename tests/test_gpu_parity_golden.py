@@ -211,6 +211,59 @@ def test_coupled_step_sees_state_written_between_steps():
     assert eng._last_dt == dt and eng._last_n_sub == n_sub
 
 
+def test_coupled_step_takes_the_2d_rate_from_its_last_step_while_the_state_is_unchanged():
+    """The 2-D CFL rates at the start of a coupled step are those the last step's own
+    last stage formed (no reduction) while h, hu and hv are unwritten: equal, in
+    float64, to a fresh reduction of the same state.  A write through torch or by a
+    standalone exchange makes the next step reduce afresh, and its dt is that of the
+    written state."""
+    from his_gb300.coupling import CoupledEngine, exchange
+    fx_x = H.load("exchange_overtop")
+    fx = H.load("coupled_overtop")
+    spec = GC.COUPLED_CASES["coupled_overtop"]
+    one, two, links, p = H.cuda_overtop(fx_x)
+    two.set_state(fx["h0"])
+    one.A = torch.as_tensor(fx["A0"])
+    one.Q = torch.as_tensor(fx["Q0"])
+    eng = CoupledEngine(two, one, p.cfg, rain=GC.rain_fn_coupled(spec), links=links)
+    t = 0.0
+    for _ in range(3):
+        t = eng.step(t, spec["t_end"])
+    calls, pairs = [], []
+    step_rate, reduce = two.step_rate_async, two.rates_async
+
+    def from_step(out, stream=None):
+        calls.append("step")
+        step_rate(out, stream)
+        fresh = torch.empty(out.shape, dtype=torch.float64, pin_memory=True)
+        reduce(fresh, stream)                   # behind the copy on the same stream
+        pairs.append((out, fresh))
+
+    def reduced(out, stream=None):
+        calls.append("reduce")
+        reduce(out, stream)
+
+    two.step_rate_async, two.rates_async = from_step, reduced
+    for _ in range(3):                          # unchanged state: the step's own rates
+        t = eng.step(t, spec["t_end"])
+        out, fresh = pairs[-1]
+        assert calls[-1] == "step" and torch.equal(out.clone(), fresh)
+
+    def expected(t):
+        return min(two.dt_from_rate(float(two.member_rates().max())), spec["t_end"] - t)
+
+    two.h = two.h * 1.5                         # written through torch
+    dt = expected(t)
+    t = eng.step(t, spec["t_end"])
+    assert calls[-1] == "reduce" and eng._last_dt == dt
+    t = eng.step(t, spec["t_end"])
+    assert calls[-1] == "step"
+    exchange(one, two, links, 30.0, p.cfg)      # the library writes h itself
+    dt = expected(t)
+    t = eng.step(t, spec["t_end"])
+    assert calls[-1] == "reduce" and eng._last_dt == dt
+
+
 def test_batched_coupled_engine_matches_reference():
     """The batched drop-in CoupledEngine (two members with their own roughness,
     channel conveyance, states, inflow and rain; one shared CFL step) against the
