@@ -38,3 +38,16 @@ def test_bad_arguments_map_to_value_error_without_a_gpu():
         assert "order" in str(e)
     else:
         raise AssertionError("expected ValueError")
+
+
+def test_asynchronous_entry_points_refuse_missing_arguments_without_a_gpu():
+    """Null handles and outputs are refused before any device call (HIS_ERR_BAD_ARG,
+    with a message naming what is missing)."""
+    lib = _lib.load()
+    for name, args in (("his_grid_step_rate_async", (None, None, None)),
+                       ("his_grid_max_rate_async", (None, None, None)),
+                       ("his_grid_step_ledger_async", (None, None, None, None)),
+                       ("his_net_step_ledger_async", (None, 0.5, 1, None, None, None))):
+        rc = getattr(lib, name)(*args)
+        assert rc == _lib.HIS_ERR_BAD_ARG, name
+        assert "required" in _lib.last_error(), (name, _lib.last_error())
